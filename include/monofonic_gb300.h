@@ -1,0 +1,126 @@
+/*
+ * monofonic_gb300.h -- C ABI of libmfgpu, the GB300 (sm_103a) implementation
+ * of monofonIC's nLPT field pipeline.
+ *
+ * Every entry point returns an int status (MF_OK = 0) and never traps on the
+ * device; the message of the last failure on a context is available through
+ * mf_last_error().  Handles own device memory.  A context is driven by one
+ * host thread at a time; all work is queued on the context's CUDA stream.
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the monofonIC source tree).
+ */
+#ifndef MONOFONIC_GB300_H
+#define MONOFONIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes: the reference throws std::runtime_error or calls abort()
+ * (src/main.cc:242-252, src/grid_fft.cc:145); here every failure is a code */
+enum {
+  MF_OK = 0,
+  MF_ERR_ARG = 1,       /* invalid argument or unsupported option */
+  MF_ERR_SHAPE = 2,     /* unsupported or mismatching grid size */
+  MF_ERR_OOM = 3,       /* device or pinned host allocation failed */
+  MF_ERR_CUDA = 4,      /* a CUDA call failed */
+  MF_ERR_TIMEOUT = 5,   /* a bounded wait ran out */
+  MF_ERR_CANCELLED = 6, /* request cancelled */
+  MF_ERR_STATE = 7      /* object in the wrong state for the call */
+};
+
+/* arithmetic of a grid: plain FP64, or the FP32-bulk form */
+enum { MF_PREC_F64 = 0, MF_PREC_F32 = 1 };
+/* space of a grid (include/grid_fft.hh:29 space_t) */
+enum { MF_SPACE_R = 0, MF_SPACE_K = 1 };
+/* convolver type (CMakeLists.txt:209-216 CONVOLVER_TYPE) */
+enum { MF_CONV_ORSZAG = 0, MF_CONV_NAIVE = 1 };
+/* operand k-space factors (include/convolution.hh:74-292) */
+enum {
+  MF_OPND_PLAIN = 0, /* f                                   multiply_field   */
+  MF_OPND_HESS = 1,  /* (i g_a)(i g_b) f                    convolve_Hessians */
+  MF_OPND_SUM = 2,   /* ((i g_a)(i g_b)+(i g_c)(i g_d)) f    SumOfHessians     */
+  MF_OPND_DIFF = 3,  /* ((i g_a)(i g_b)-(i g_c)(i g_d)) f    DifferenceOfHessians */
+  MF_OPND_GRAD = 4   /* (i g_a) f                           convolve_Gradients */
+};
+/* output operators (include/operators.hh:25-35) */
+enum { MF_OP_ASSIGN = 0, MF_OP_ADD = 1, MF_OP_SUB = 2, MF_OP_AXPY = 3 };
+/* particle loads (include/particle_generator.hh:31-39) */
+enum { MF_LATTICE_SC = 0, MF_LATTICE_BCC = 1, MF_LATTICE_FCC = 2, MF_LATTICE_RSC = 3 };
+
+typedef struct mf_ctx mf_ctx;
+typedef struct mf_grid mf_grid;
+typedef struct mf_conv mf_conv;
+
+/* ---- context ----------------------------------------------------------- */
+/* replaces the process-level set-up of src/main.cc:150-181 (FFTW/OpenMP init) */
+int mf_ctx_create(int device, mf_ctx** out);
+int mf_ctx_destroy(mf_ctx* ctx);
+const char* mf_last_error(const mf_ctx* ctx);
+int mf_ctx_synchronize(mf_ctx* ctx);
+/* library version string */
+const char* mf_version(void);
+/* 1 if grid size n is supported by the compiled kernels */
+int mf_grid_size_supported(int n);
+
+/* ---- Grid_FFT<real_t> (include/grid_fft.hh:40-914) --------------------- */
+/* Grid_FFT ctor + allocate (grid_fft.hh:77-83, src/grid_fft.cc:40-112):
+ * n^3 grid of box length boxlen, padded in-place layout of (n+2)*n*n reals */
+int mf_grid_create(mf_ctx* ctx, int n, double boxlen, int prec, int space, mf_grid** out);
+int mf_grid_destroy(mf_grid* g);
+/* size(), space_, data_ and the byte size of the padded array */
+int mf_grid_info(const mf_grid* g, int* n, int* prec, int* space, void** dptr, size_t* bytes);
+/* copy the whole padded array (ntot_ reals of the grid's precision) from /
+ * to host memory; upload sets the space flag (relem/kelem host access) */
+int mf_grid_upload(mf_grid* g, const void* host, int space);
+int mf_grid_download(mf_grid* g, void* host);
+/* upload a real-space FP64 array of n^3 values (no padding), converting to
+ * the grid's precision (RNG_plugin::Fill_Grid, include/random_plugin.hh:37) */
+int mf_grid_fill_real64(mf_grid* g, const double* host_n3);
+/* FourierTransformForward/Backward(do_transform) (src/grid_fft.cc:208-270) */
+int mf_grid_fft_forward(mf_grid* g, int do_transform);
+int mf_grid_fft_backward(mf_grid* g, int do_transform);
+/* zero() (grid_fft.hh:150-155) */
+int mf_grid_zero(mf_grid* g);
+/* operator*= (grid_fft.hh:392-403) */
+int mf_grid_scale(mf_grid* g, double x);
+/* zero_DC_mode, k-space branch (grid_fft.hh:844-850) */
+int mf_grid_zero_dc(mf_grid* g);
+/* apply_InverseLaplacian (grid_fft.hh:440-449) */
+int mf_grid_inverse_laplacian(mf_grid* g);
+/* shift_field (grid_fft.hh:832-842) */
+int mf_grid_shift(mf_grid* g, const double s[3], int transform_back);
+/* Compute_PowerSpectrum (src/grid_fft.cc:1133-1210); arrays of nbins_cap,
+ * *nbins receives int(kmax/kmin) */
+int mf_grid_power_spectrum(mf_grid* g, double* bin_k, double* bin_P, double* bin_eP,
+                           int64_t* bin_count, int nbins_cap, int* nbins);
+
+/* ---- convolvers (include/convolution.hh) ------------------------------- */
+typedef struct {
+  mf_grid* grid; /* k-space input field */
+  int kind;      /* MF_OPND_* */
+  int d[4];      /* directions a, b, c, d */
+} mf_operand;
+
+/* OrszagConvolver / NaiveConvolver ctor (convolution.hh:463-495, 318-323) */
+int mf_conv_create(mf_ctx* ctx, int n, double boxlen, int prec, int kind, mf_conv** out);
+int mf_conv_destroy(mf_conv* cv);
+/* convolve2 (convolution.hh:513-535 / 328-356) with output operator op
+ * applied to out (x is the multiply_add_to factor) */
+int mf_conv_convolve2(mf_conv* cv, const mf_operand* a, const mf_operand* b, mf_grid* out, int op, double x);
+/* convolve3 (convolution.hh:543-549 / 359-402) */
+int mf_conv_convolve3(mf_conv* cv, const mf_operand* a, const mf_operand* b, const mf_operand* c,
+                      mf_grid* out, int op, double x);
+/* convolve2 followed by apply_InverseLaplacian of out, fused (the last
+ * source term of phi(2), phi(3), A(3); src/ic_generator.cc:488,528,545) */
+int mf_conv_convolve2_invlap(mf_conv* cv, const mf_operand* a, const mf_operand* b, mf_grid* out, int op,
+                             double x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MONOFONIC_GB300_H */

@@ -1,0 +1,256 @@
+"""monofonic_gb300: GB300 (sm_103a) nLPT field pipeline of monofonIC.
+
+Python mirror of the reference's field/convolver/operator API over the C ABI
+of libmfgpu (include/monofonic_gb300.h):
+
+    Grid_FFT            include/grid_fft.hh:40-914
+    OrszagConvolver     include/convolution.hh:429-669
+    NaiveConvolver      include/convolution.hh:296-426
+    op.assign_to ...    include/operators.hh:25-35
+
+All arithmetic runs in CUDA kernels; the Python layer only moves handles.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import MFError
+
+__all__ = ["Context", "Grid_FFT", "OrszagConvolver", "NaiveConvolver", "op", "MFError", "lib"]
+
+
+def lib():
+    return L.load()
+
+
+def _check(ctx_ptr, rc):
+    if rc != L.MF_OK:
+        msg = lib().mf_last_error(ctx_ptr)
+        raise MFError(rc, msg.decode() if msg else "")
+
+
+_PREC = {"f64": L.MF_PREC_F64, "f32": L.MF_PREC_F32, "double": L.MF_PREC_F64, "float": L.MF_PREC_F32}
+
+
+class Context:
+    """A device context: one CUDA stream, twiddle tables, error state."""
+
+    def __init__(self, device: int = 0):
+        p = C.c_void_p()
+        rc = lib().mf_ctx_create(device, C.byref(p))
+        if rc != L.MF_OK:
+            raise MFError(rc, f"mf_ctx_create(device={device}) failed")
+        self.ptr = p
+
+    def synchronize(self):
+        _check(self.ptr, lib().mf_ctx_synchronize(self.ptr))
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().mf_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Grid_FFT:
+    """Device-resident Grid_FFT<real_t>: n^3 real grid in the padded in-place
+    layout (n+2)*n*n reals, k-space (n, n, n/2+1) complex in place."""
+
+    def __init__(self, ctx: Context, n: int, boxlen: float, prec: str = "f64", space: str = "r"):
+        self.ctx, self.n, self.L = ctx, int(n), float(boxlen)
+        self.prec = prec
+        self.dtype = np.float64 if _PREC[prec] == L.MF_PREC_F64 else np.float32
+        self.cdtype = np.complex128 if self.dtype == np.float64 else np.complex64
+        p = C.c_void_p()
+        sp = L.MF_SPACE_K if space == "k" else L.MF_SPACE_R
+        _check(ctx.ptr, lib().mf_grid_create(ctx.ptr, self.n, self.L, _PREC[prec], sp, C.byref(p)))
+        self.ptr = p
+
+    # -- state ------------------------------------------------------------
+    @property
+    def space(self):
+        s = C.c_int()
+        lib().mf_grid_info(self.ptr, None, None, C.byref(s), None, None)
+        return "k" if s.value == L.MF_SPACE_K else "r"
+
+    def device_ptr(self):
+        d = C.c_void_p()
+        lib().mf_grid_info(self.ptr, None, None, None, C.byref(d), None)
+        return d.value
+
+    # -- host transfer ------------------------------------------------------
+    def upload_padded(self, arr: np.ndarray, space: str):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        assert a.size == (self.n + 2) * self.n * self.n
+        _check(self.ctx.ptr, lib().mf_grid_upload(self.ptr, a.ctypes.data, L.MF_SPACE_K if space == "k" else L.MF_SPACE_R))
+
+    def download_padded(self) -> np.ndarray:
+        a = np.empty((self.n, self.n, self.n + 2), dtype=self.dtype)
+        _check(self.ctx.ptr, lib().mf_grid_download(self.ptr, a.ctypes.data))
+        return a
+
+    def set_real(self, x: np.ndarray):
+        """relem assignment of an (n,n,n) array (host upload)."""
+        a = np.zeros((self.n, self.n, self.n + 2), dtype=self.dtype)
+        a[:, :, : self.n] = x
+        self.upload_padded(a, "r")
+
+    def fill_real64(self, x: np.ndarray):
+        """RNG_plugin::Fill_Grid equivalent: upload an (n,n,n) float64 field."""
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        assert a.shape == (self.n,) * 3
+        _check(self.ctx.ptr, lib().mf_grid_fill_real64(self.ptr, a.ctypes.data))
+
+    def set_k(self, X: np.ndarray):
+        """kelem assignment of an (n,n,n/2+1) complex array (host upload)."""
+        a = np.ascontiguousarray(X, dtype=self.cdtype)
+        self.upload_padded(a.view(self.dtype).reshape(self.n, self.n, self.n + 2), "k")
+
+    def get_real(self) -> np.ndarray:
+        return self.download_padded()[:, :, : self.n].copy()
+
+    def get_k(self) -> np.ndarray:
+        return self.download_padded().view(self.cdtype).reshape(self.n, self.n, self.n // 2 + 1).copy()
+
+    # -- Grid_FFT methods ---------------------------------------------------
+    def FourierTransformForward(self, do_transform: bool = True):
+        _check(self.ctx.ptr, lib().mf_grid_fft_forward(self.ptr, int(do_transform)))
+
+    def FourierTransformBackward(self, do_transform: bool = True):
+        _check(self.ctx.ptr, lib().mf_grid_fft_backward(self.ptr, int(do_transform)))
+
+    def zero(self):
+        _check(self.ctx.ptr, lib().mf_grid_zero(self.ptr))
+
+    def __imul__(self, x: float):
+        _check(self.ctx.ptr, lib().mf_grid_scale(self.ptr, float(x)))
+        return self
+
+    def zero_DC_mode(self):
+        _check(self.ctx.ptr, lib().mf_grid_zero_dc(self.ptr))
+
+    def apply_InverseLaplacian(self):
+        _check(self.ctx.ptr, lib().mf_grid_inverse_laplacian(self.ptr))
+
+    def shift_field(self, s, transform_back: bool = True):
+        arr = (C.c_double * 3)(*[float(v) for v in s])
+        _check(self.ctx.ptr, lib().mf_grid_shift(self.ptr, arr, int(transform_back)))
+
+    def Compute_PowerSpectrum(self):
+        cap = self.n
+        k, P, eP = (np.zeros(cap) for _ in range(3))
+        cnt = np.zeros(cap, dtype=np.int64)
+        nb = C.c_int()
+        _check(self.ctx.ptr, lib().mf_grid_power_spectrum(self.ptr, k.ctypes.data, P.ctypes.data, eP.ctypes.data,
+                                                          cnt.ctypes.data, cap, C.byref(nb)))
+        m = nb.value
+        return k[:m], P[:m], eP[:m], cnt[:m]
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().mf_grid_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Op:
+    """Output operator descriptor (include/operators.hh:25-35)."""
+
+    def __init__(self, grid, kind, x=1.0):
+        self.grid, self.kind, self.x = grid, kind, x
+
+
+class op:
+    @staticmethod
+    def assign_to(g):
+        return _Op(g, L.MF_OP_ASSIGN)
+
+    @staticmethod
+    def add_to(g):
+        return _Op(g, L.MF_OP_ADD)
+
+    @staticmethod
+    def subtract_from(g):
+        return _Op(g, L.MF_OP_SUB)
+
+    @staticmethod
+    def multiply_add_to(g, x):
+        return _Op(g, L.MF_OP_AXPY, float(x))
+
+
+def _opnd(g, kind, d=()):
+    o = L.mf_operand()
+    o.grid = g.ptr
+    o.kind = kind
+    for i, v in enumerate(d):
+        o.d[i] = int(v)
+    return o
+
+
+class _Convolver:
+    KIND = L.MF_CONV_ORSZAG
+
+    def __init__(self, ctx: Context, n: int, boxlen: float, prec: str = "f64"):
+        self.ctx = ctx
+        p = C.c_void_p()
+        _check(ctx.ptr, lib().mf_conv_create(ctx.ptr, int(n), float(boxlen), _PREC[prec], self.KIND, C.byref(p)))
+        self.ptr = p
+
+    def _c2(self, a, b, o: _Op, invlap=False):
+        fn = lib().mf_conv_convolve2_invlap if invlap else lib().mf_conv_convolve2
+        _check(self.ctx.ptr, fn(self.ptr, C.byref(a), C.byref(b), o.grid.ptr, o.kind, o.x))
+
+    # BaseConvolver API (convolution.hh:74-292)
+    def convolve_Gradients(self, inl, d1l, inr, d1r, o, invlap=False):
+        self._c2(_opnd(inl, L.MF_OPND_GRAD, d1l), _opnd(inr, L.MF_OPND_GRAD, d1r), o, invlap)
+
+    def convolve_Hessians(self, inl, d2l, inm, d2m, *rest, invlap=False):
+        if len(rest) == 1:
+            self._c2(_opnd(inl, L.MF_OPND_HESS, d2l), _opnd(inm, L.MF_OPND_HESS, d2m), rest[0], invlap)
+        else:
+            inr, d2r, o = rest
+            a, b, c = (_opnd(inl, L.MF_OPND_HESS, d2l), _opnd(inm, L.MF_OPND_HESS, d2m),
+                       _opnd(inr, L.MF_OPND_HESS, d2r))
+            _check(self.ctx.ptr, lib().mf_conv_convolve3(self.ptr, C.byref(a), C.byref(b), C.byref(c),
+                                                         o.grid.ptr, o.kind, o.x))
+
+    def convolve_SumOfHessians(self, inl, d2l, inr, d2r1, d2r2, o, invlap=False):
+        self._c2(_opnd(inl, L.MF_OPND_HESS, d2l), _opnd(inr, L.MF_OPND_SUM, tuple(d2r1) + tuple(d2r2)), o, invlap)
+
+    def convolve_DifferenceOfHessians(self, inl, d2l, inr, d2r1, d2r2, o, invlap=False):
+        self._c2(_opnd(inl, L.MF_OPND_HESS, d2l), _opnd(inr, L.MF_OPND_DIFF, tuple(d2r1) + tuple(d2r2)), o, invlap)
+
+    def multiply_field(self, inl, inr, o):
+        self._c2(_opnd(inl, L.MF_OPND_PLAIN), _opnd(inr, L.MF_OPND_PLAIN), o)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().mf_conv_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OrszagConvolver(_Convolver):
+    KIND = L.MF_CONV_ORSZAG
+
+
+class NaiveConvolver(_Convolver):
+    KIND = L.MF_CONV_NAIVE

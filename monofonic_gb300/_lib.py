@@ -1,0 +1,86 @@
+"""ctypes binding of libmfgpu (the C ABI declared in include/monofonic_gb300.h).
+
+The library is loaded from the package directory.  There is no fallback: if
+the shared object is missing or fails to load, importing raises, so nothing
+silently runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmfgpu.so")
+
+MF_OK, MF_ERR_ARG, MF_ERR_SHAPE, MF_ERR_OOM, MF_ERR_CUDA, MF_ERR_TIMEOUT, MF_ERR_CANCELLED, MF_ERR_STATE = range(8)
+MF_PREC_F64, MF_PREC_F32 = 0, 1
+MF_SPACE_R, MF_SPACE_K = 0, 1
+MF_CONV_ORSZAG, MF_CONV_NAIVE = 0, 1
+MF_OPND_PLAIN, MF_OPND_HESS, MF_OPND_SUM, MF_OPND_DIFF, MF_OPND_GRAD = range(5)
+MF_OP_ASSIGN, MF_OP_ADD, MF_OP_SUB, MF_OP_AXPY = range(4)
+
+ERROR_NAMES = {1: "MF_ERR_ARG", 2: "MF_ERR_SHAPE", 3: "MF_ERR_OOM", 4: "MF_ERR_CUDA",
+               5: "MF_ERR_TIMEOUT", 6: "MF_ERR_CANCELLED", 7: "MF_ERR_STATE"}
+
+
+class mf_operand(C.Structure):
+    _fields_ = [("grid", C.c_void_p), ("kind", C.c_int), ("d", C.c_int * 4)]
+
+
+# name -> (restype, argtypes); every C-ABI symbol the header declares
+SIGNATURES = {
+    "mf_version": (C.c_char_p, []),
+    "mf_grid_size_supported": (C.c_int, [C.c_int]),
+    "mf_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "mf_last_error": (C.c_char_p, [C.c_void_p]),
+    "mf_ctx_synchronize": (C.c_int, [C.c_void_p]),
+    "mf_grid_create": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_grid_destroy": (C.c_int, [C.c_void_p]),
+    "mf_grid_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                               C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]),
+    "mf_grid_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "mf_grid_download": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mf_grid_fill_real64": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mf_grid_fft_forward": (C.c_int, [C.c_void_p, C.c_int]),
+    "mf_grid_fft_backward": (C.c_int, [C.c_void_p, C.c_int]),
+    "mf_grid_zero": (C.c_int, [C.c_void_p]),
+    "mf_grid_scale": (C.c_int, [C.c_void_p, C.c_double]),
+    "mf_grid_zero_dc": (C.c_int, [C.c_void_p]),
+    "mf_grid_inverse_laplacian": (C.c_int, [C.c_void_p]),
+    "mf_grid_shift": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
+    "mf_grid_power_spectrum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.POINTER(C.c_int)]),
+    "mf_conv_create": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_conv_destroy": (C.c_int, [C.c_void_p]),
+    "mf_conv_convolve2": (C.c_int, [C.c_void_p, C.POINTER(mf_operand), C.POINTER(mf_operand), C.c_void_p,
+                                    C.c_int, C.c_double]),
+    "mf_conv_convolve2_invlap": (C.c_int, [C.c_void_p, C.POINTER(mf_operand), C.POINTER(mf_operand), C.c_void_p,
+                                           C.c_int, C.c_double]),
+    "mf_conv_convolve3": (C.c_int, [C.c_void_p, C.POINTER(mf_operand), C.POINTER(mf_operand),
+                                    C.POINTER(mf_operand), C.c_void_p, C.c_int, C.c_double]),
+}
+
+_lib = None
+
+
+def load():
+    """Load libmfgpu.so (raises OSError/ImportError if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libmfgpu.so not built at {LIB_PATH}; run monofonic_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class MFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code

@@ -1,0 +1,249 @@
+// Device FFT machinery for the nLPT field pipeline (sm_103a).
+//
+// A line FFT of compile-time length L = 2^a 3^b is a Stockham auto-sort
+// decimation-in-time transform.  Every thread of a line owns E = L/TPL
+// elements in registers; each stage is a set of radix-R butterflies computed
+// in registers, and consecutive stages exchange data through shared memory.
+// The first stage reads its inputs through a caller-supplied loader and the
+// last stage hands its outputs to a caller-supplied storer, so padding,
+// Hessian factors, products, unpadding and output operators fuse into the
+// FFT's global-memory loads and stores.
+//
+// Stage s (radix R, Lc = product of earlier radices), butterfly b in [0,L/R):
+//   k = b mod Lc; x_p = in[b + p L/R] * w_L^(p k L/(Lc R)); X = DFT_R(x);
+//   out[(b-k) R + k + q Lc] = X_q.
+// Stage-0 inputs are in[b + p L/R0]; last-stage outputs are out[b + q L/Rl].
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace mf {
+
+template <typename T> struct cplx_of;
+template <> struct cplx_of<float> { using type = float2; };
+template <> struct cplx_of<double> { using type = double2; };
+template <typename T> using cplx = typename cplx_of<T>::type;
+
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> mkc(T x, T y) { cplx<T> r; r.x = x; r.y = y; return r; }
+template <typename C>
+__device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C b) { C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
+// a * conj(b)
+template <typename C>
+__device__ __forceinline__ C cmulc(C a, C b) { C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r; }
+template <typename C, typename T>
+__device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C>
+__device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV, typename C>
+__device__ __forceinline__ C cmul_mi(C a) { C r; if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; } return r; }
+
+// ---------------------------------------------------------------------------
+// small DFTs, forward sign e^{-2 pi i pq/R}, inverse e^{+2 pi i pq/R}
+// ---------------------------------------------------------------------------
+template <typename T, bool INV>
+__device__ __forceinline__ void dft2(cplx<T>* a) {
+  cplx<T> t = a[0];
+  a[0] = cadd(t, a[1]);
+  a[1] = csub(t, a[1]);
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft4v(cplx<T>& a0, cplx<T>& a1, cplx<T>& a2, cplx<T>& a3) {
+  cplx<T> t0 = cadd(a0, a2), t1 = csub(a0, a2), t2 = cadd(a1, a3), t3 = cmul_mi<INV>(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft4(cplx<T>* a) { dft4v<T, INV>(a[0], a[1], a[2], a[3]); }
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft3(cplx<T>* a) {
+  const T c = T(0.86602540378443864676372317075294);  // sqrt(3)/2
+  cplx<T> s = cadd(a[1], a[2]), d = csub(a[1], a[2]);
+  cplx<T> m = mkc<T>(a[0].x - T(0.5) * s.x, a[0].y - T(0.5) * s.y);
+  a[0] = cadd(a[0], s);
+  // (-i c) d forward, (+i c) d inverse
+  cplx<T> r = cmul_mi<INV>(d);
+  r.x *= c; r.y *= c;
+  a[1] = cadd(m, r);
+  a[2] = csub(m, r);
+}
+
+template <typename T, bool INV>
+__device__ __forceinline__ void dft8(cplx<T>* a) {
+  const T h = T(0.70710678118654752440084436210485);  // 1/sqrt(2)
+  cplx<T> e0 = a[0], e1 = a[2], e2 = a[4], e3 = a[6];
+  cplx<T> o0 = a[1], o1 = a[3], o2 = a[5], o3 = a[7];
+  dft4v<T, INV>(e0, e1, e2, e3);
+  dft4v<T, INV>(o0, o1, o2, o3);
+  // twiddle the odd half by w8^q
+  cplx<T> w1, w2, w3;
+  if (!INV) {
+    w1 = mkc<T>((o1.x + o1.y) * h, (o1.y - o1.x) * h);
+    w2 = mkc<T>(o2.y, -o2.x);
+    w3 = mkc<T>((o3.y - o3.x) * h, -(o3.x + o3.y) * h);
+  } else {
+    w1 = mkc<T>((o1.x - o1.y) * h, (o1.x + o1.y) * h);
+    w2 = mkc<T>(-o2.y, o2.x);
+    w3 = mkc<T>(-(o3.x + o3.y) * h, (o3.x - o3.y) * h);
+  }
+  a[0] = cadd(e0, o0); a[4] = csub(e0, o0);
+  a[1] = cadd(e1, w1); a[5] = csub(e1, w1);
+  a[2] = cadd(e2, w2); a[6] = csub(e2, w2);
+  a[3] = cadd(e3, w3); a[7] = csub(e3, w3);
+}
+
+template <typename T, bool INV, int R>
+__device__ __forceinline__ void dftR(cplx<T>* a) {
+  if constexpr (R == 2) dft2<T, INV>(a);
+  else if constexpr (R == 3) dft3<T, INV>(a);
+  else if constexpr (R == 4) dft4<T, INV>(a);
+  else if constexpr (R == 8) dft8<T, INV>(a);
+  else static_assert(R == 2, "unsupported radix");
+}
+
+// ---------------------------------------------------------------------------
+// compile-time plans: L -> radix list (8s first, then 4/2, then 3s)
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int ilog2_part(int L) { int a = 0; while (L % 2 == 0) { L /= 2; ++a; } return a; }
+__host__ __device__ constexpr int i3_part(int L) { int b = 0; while (L % 3 == 0) { L /= 3; ++b; } return b; }
+__host__ __device__ constexpr bool plan_ok(int L) {
+  int x = L; while (x % 2 == 0) x /= 2; while (x % 3 == 0) x /= 3; return x == 1 && L >= 4;
+}
+__host__ __device__ constexpr int plan_nstages(int L, int maxr) {
+  int a = ilog2_part(L), b = i3_part(L), n = b;
+  int r8 = (maxr >= 8) ? a / 3 : 0;
+  int rem = a - 3 * r8;
+  n += r8;
+  while (rem > 0) { int t = (rem >= 2 && maxr >= 4) ? 2 : 1; rem -= t; ++n; }
+  return n;
+}
+__host__ __device__ constexpr int plan_radix(int L, int maxr, int s) {
+  int a = ilog2_part(L), b = i3_part(L);
+  int r8 = (maxr >= 8) ? a / 3 : 0;
+  int rem = a - 3 * r8;
+  int idx = 0;
+  for (int i = 0; i < r8; ++i) { if (idx == s) return 8; ++idx; }
+  while (rem > 0) { int t = (rem >= 2 && maxr >= 4) ? 2 : 1; rem -= t; if (idx == s) return 1 << t; ++idx; }
+  for (int i = 0; i < b; ++i) { if (idx == s) return 3; ++idx; }
+  return 1;
+}
+__host__ __device__ constexpr int plan_elems(int L, int maxr) {
+  // lcm of the radices
+  int e = 1;
+  for (int s = 0; s < plan_nstages(L, maxr); ++s) {
+    int r = plan_radix(L, maxr, s);
+    int g = e, h = r; while (h) { int t = g % h; g = h; h = t; }
+    e = e / g * r;
+  }
+  return e;
+}
+__host__ __device__ constexpr int plan_lcur(int L, int maxr, int s) {
+  int p = 1; for (int i = 0; i < s; ++i) p *= plan_radix(L, maxr, i); return p;
+}
+
+// Line FFT of length L in precision T, direction INV, radices up to MAXR.
+template <typename T, int L, bool INV, int MAXR = 8>
+struct LineFFT {
+  static_assert(plan_ok(L), "FFT length must be 2^a 3^b >= 4");
+  using C = cplx<T>;
+  static constexpr int NS = plan_nstages(L, MAXR);
+  static constexpr int E = plan_elems(L, MAXR);
+  static constexpr int TPL = L / E;
+  static constexpr int R0 = plan_radix(L, MAXR, 0);
+  static constexpr int RL = plan_radix(L, MAXR, NS - 1);
+
+  // stage-0 input element index of register slot (m*R0 + p)
+  __device__ static __forceinline__ int in_index(int t, int slot) {
+    return t + (slot / R0) * TPL + (slot % R0) * (L / R0);
+  }
+  // last-stage output element index of register slot (m*RL + q)
+  __device__ static __forceinline__ int out_index(int t, int slot) {
+    return t + (slot / RL) * TPL + (slot % RL) * (L / RL);
+  }
+
+  template <int S>
+  __device__ static __forceinline__ void compute(C (&v)[E], int t, const C* __restrict__ tw) {
+    constexpr int R = plan_radix(L, MAXR, S);
+    constexpr int LC = plan_lcur(L, MAXR, S);
+    constexpr int NB = E / R;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+      if constexpr (LC > 1) {
+        const int b = t + m * TPL;
+        const int k = b % LC;
+        constexpr int STR = L / (LC * R);
+#pragma unroll
+        for (int p = 1; p < R; ++p) {
+          const C w = tw[p * k * STR];
+          v[m * R + p] = INV ? cmulc(v[m * R + p], w) : cmul(v[m * R + p], w);
+        }
+      }
+      dftR<T, INV, R>(&v[m * R]);
+    }
+  }
+
+  // write stage-S outputs to shared memory (element e at sm[e*cs])
+  template <int S>
+  __device__ static __forceinline__ void write_out(const C (&v)[E], int t, C* sm, int cs) {
+    constexpr int R = plan_radix(L, MAXR, S);
+    constexpr int LC = plan_lcur(L, MAXR, S);
+    constexpr int NB = E / R;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+      const int b = t + m * TPL;
+      const int k = b % LC;
+      const int base = (b - k) * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) sm[(base + q * LC) * cs] = v[m * R + q];
+    }
+  }
+
+  // read stage-S inputs from shared memory
+  template <int S>
+  __device__ static __forceinline__ void read_in(C (&v)[E], int t, const C* sm, int cs) {
+    constexpr int R = plan_radix(L, MAXR, S);
+    constexpr int NB = E / R;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+      const int b = t + m * TPL;
+#pragma unroll
+      for (int p = 0; p < R; ++p) v[m * R + p] = sm[(b + p * (L / R)) * cs];
+    }
+  }
+
+  template <int S, class SYNC>
+  __device__ static __forceinline__ void run_from(C (&v)[E], int t, C* sm, int cs, const C* __restrict__ tw, SYNC sync) {
+    if constexpr (S < NS) {
+      sync();
+      write_out<S - 1>(v, t, sm, cs);
+      sync();
+      read_in<S>(v, t, sm, cs);
+      compute<S>(v, t, tw);
+      run_from<S + 1>(v, t, sm, cs, tw, sync);
+    }
+  }
+
+  // v holds stage-0 inputs on entry and last-stage outputs on exit.  The
+  // shared buffer (L elements at stride cs) may be overwritten; a sync is
+  // issued before the first write, so callers may have read it just before.
+  template <class SYNC>
+  __device__ static __forceinline__ void run(C (&v)[E], int t, C* sm, int cs, const C* __restrict__ tw, SYNC sync) {
+    compute<0>(v, t, tw);
+    run_from<1>(v, t, sm, cs, tw, sync);
+  }
+};
+
+struct SyncBlock { __device__ __forceinline__ void operator()() const { __syncthreads(); } };
+
+}  // namespace mf

@@ -1,0 +1,178 @@
+// Launch configuration and per-length dispatch of the FFT pass kernels.
+// Each translation unit mf_fft_<part>_<prec>.cu defines MF_T and one MF_PART_*
+// macro and includes this file, so the instantiations compile in parallel.
+#pragma once
+
+#include "mf_internal.h"
+#include "mf_kernels.cuh"
+
+namespace mf {
+
+// columns per CTA of a strided pass: 128-byte rows (16 float2 / 8 double2),
+// at most 1024 threads, at least 128 threads
+template <typename T, int L>
+constexpr int col_ncol() {
+  constexpr int tpl = LineFFT<T, L, false>::TPL;
+  int nc = (sizeof(T) == 4) ? 16 : 8;
+  while (nc * tpl > 1024) nc /= 2;
+  while (nc * tpl < 128 && nc < 64) nc *= 2;
+  return nc;
+}
+
+// lines per CTA of a z pass, bounded by ~100 KB of shared memory per CTA
+template <typename T, int H, int SMEM_ELEMS_PER_LINE>
+constexpr int z_lpb() {
+  constexpr int tpl = LineFFT<T, H, false>::TPL;
+  int l = 256 / tpl;
+  if (l < 1) l = 1;
+  while (l > 1 && (size_t)l * SMEM_ELEMS_PER_LINE * sizeof(cplx<T>) > 100 * 1024) l /= 2;
+  return l;
+}
+
+template <typename K>
+inline cudaError_t set_smem(K kern, size_t smem) {
+  if (smem > 48 * 1024) return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
+}
+
+template <typename T, int L, bool INV, class OP>
+cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s) {
+  constexpr int NC = col_ncol<T, L>();
+  constexpr int TPL = LineFFT<T, L, INV>::TPL;
+  const size_t smem = (size_t)L * NC * sizeof(cplx<T>);
+  auto kern = k_colfft<T, L, INV, NC, OP>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, nz);
+  kern<<<grid, block, smem, s>>>(op, tw, ncols);
+  return cudaGetLastError();
+}
+
+template <typename T, int H, class OP>
+cudaError_t launch_zr2c(OP op, int nlines, int kout, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
+  constexpr int LPB = z_lpb<T, H, H + 1>();
+  constexpr int TPL = LineFFT<T, H, false>::TPL;
+  const size_t smem = (size_t)LPB * (H + 1) * sizeof(cplx<T>);
+  auto kern = k_zr2c<T, H, TPL * LPB, OP>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  dim3 block(TPL, LPB), grid((nlines + LPB - 1) / LPB);
+  kern<<<grid, block, smem, s>>>(op, twH, twM, nlines, kout);
+  return cudaGetLastError();
+}
+
+template <typename T, int H, class OP>
+cudaError_t launch_zc2r(OP op, int nlines, int kin, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
+  constexpr int LPB = z_lpb<T, H, H + 1>();
+  constexpr int TPL = LineFFT<T, H, true>::TPL;
+  const size_t smem = (size_t)LPB * (H + 1) * sizeof(cplx<T>);
+  auto kern = k_zc2r<T, H, TPL * LPB, OP>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  dim3 block(TPL, LPB), grid((nlines + LPB - 1) / LPB);
+  kern<<<grid, block, smem, s>>>(op, twH, twM, nlines, kin);
+  return cudaGetLastError();
+}
+
+template <typename T, int H>
+cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
+  constexpr int LPB = z_lpb<T, H, 2 * H + 2>();
+  constexpr int TPL = LineFFT<T, H, true>::TPL;
+  const size_t smem = (size_t)LPB * (2 * H + 2) * sizeof(cplx<T>);
+  auto kern = k_zconv<T, H, TPL * LPB>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  dim3 block(TPL, LPB), grid((a.nlines + LPB - 1) / LPB);
+  kern<<<grid, block, smem, s>>>(a, twH, twM);
+  return cudaGetLastError();
+}
+
+// compiled lengths: N-grid passes (L = N, H = N/2) and convolution passes
+// (L = M for Orszag 3/2, M = N for the aliased convolver)
+#define MF_LEN_N(X) X(16) X(32) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
+#define MF_LEN_NH(X) X(8) X(16) X(32) X(48) X(64) X(96) X(128) X(192) X(256)
+#define MF_LEN_CONV(X) \
+  X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(144) X(192) X(256) X(288) X(384) X(512) X(576) X(768)
+#define MF_LEN_CONVH(X) \
+  X(8) X(12) X(16) X(24) X(32) X(48) X(64) X(72) X(96) X(128) X(144) X(192) X(256) X(288) X(384)
+
+#if defined(MF_PART_PLAIN)
+template <typename T>
+cudaError_t Launch<T>::colfft_plain(int L, bool inv, PlainStridedOp<T> op, int nslab, int ncols,
+                                    const cplx<T>* tw, cudaStream_t s) {
+#define CASE(LL)                                                              \
+  case LL:                                                                    \
+    return inv ? launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s)          \
+               : launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+  switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template <typename T>
+cudaError_t Launch<T>::z_r2c_plain(int H, PlainZOp<T> op, int nlines, int kout, const cplx<T>* twH,
+                                   const cplx<T>* twM, cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zr2c<T, HH>(op, nlines, kout, twH, twM, s);
+  switch (H) { MF_LEN_NH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template <typename T>
+cudaError_t Launch<T>::z_c2r_plain(int H, PlainZOp<T> op, int nlines, int kin, const cplx<T>* twH,
+                                   const cplx<T>* twM, cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zc2r<T, HH>(op, nlines, kin, twH, twM, s);
+  switch (H) { MF_LEN_NH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::colfft_plain(int, bool, PlainStridedOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::z_r2c_plain(int, PlainZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::z_c2r_plain(int, PlainZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
+#endif
+
+#if defined(MF_PART_CONVX)
+template <typename T>
+cudaError_t Launch<T>::conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
+                                 const cplx<T>* tw, cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s);
+  switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template <typename T>
+cudaError_t Launch<T>::conv_xfwd(int L, ConvXFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                 cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+  switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::conv_xinv(int, ConvXInvOp<MF_T>, int, int, int, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::conv_xfwd(int, ConvXFwdOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
+#endif
+
+#if defined(MF_PART_CONVY)
+template <typename T>
+cudaError_t Launch<T>::conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,
+                                 const cplx<T>* tw, cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s);
+  switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template <typename T>
+cudaError_t Launch<T>::conv_yfwd(int L, ConvYFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                 cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+  switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::conv_yinv(int, ConvYInvOp<MF_T>, int, int, int, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::conv_yfwd(int, ConvYFwdOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
+#endif
+
+#if defined(MF_PART_ZCONV)
+template <typename T>
+cudaError_t Launch<T>::z_conv(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
+                              cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zconv<T, HH>(a, twH, twM, s);
+  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::z_conv(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
+#endif
+
+}  // namespace mf

@@ -1,0 +1,152 @@
+// Pointwise k-space / real-space kernels on N-grids (padded in-place layout).
+#include <cmath>
+
+#include "mf_runtime.h"
+
+namespace mf {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(size_t n, int per = 1) {
+  size_t b = (n + (size_t)kThreads * per - 1) / ((size_t)kThreads * per);
+  if (b > 152u * 64u) b = 152u * 64u;
+  if (b == 0) b = 1;
+  return (unsigned)b;
+}
+
+template <typename T>
+__global__ void k_scale(T* d, size_t n, T x) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) d[i] *= x;
+}
+
+template <typename T>
+__global__ void k_zero_dc(T* d) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) { d[0] = T(0); d[1] = T(0); }
+}
+
+// apply_InverseLaplacian (grid_fft.hh:440-449): -x/k^2, then zero_DC_mode
+template <typename T>
+__global__ void k_invlap(cplx<T>* d, int n, T kfac) {
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    const T kx = kcomp<T>(i, n, kfac), ky = kcomp<T>(j, n, kfac), kk = kcomp<T>(kz, n, kfac);
+    const T k2 = kx * kx + ky * ky + kk * kk;
+    cplx<T> v = d[idx];
+    d[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(-v.x / k2, -v.y / k2);
+  }
+}
+
+// shift_field's phase (grid_fft.hh:835-838): x * exp(i (s.k) dx)
+template <typename T>
+__global__ void k_shift(cplx<T>* d, int n, T kfac, T dx, T s0, T s1, T s2) {
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    const T sh = s0 * kcomp<T>(i, n, kfac) * dx + s1 * kcomp<T>(j, n, kfac) * dx + s2 * kcomp<T>(kz, n, kfac) * dx;
+    T sn, cs;
+    if constexpr (sizeof(T) == 4) sincosf(sh, &sn, &cs); else sincos(sh, &sn, &cs);
+    d[idx] = cmul(d[idx], mkc<T>(cs, sn));
+  }
+}
+
+template <typename T>
+__global__ void k_fill_from_f64(T* d, const double* src, int n) {
+  const size_t tot = (size_t)n * n * n;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < tot; c += (size_t)gridDim.x * blockDim.x) {
+    const size_t line = c / n;
+    const int k = (int)(c % n);
+    d[line * (n + 2) + k] = T(src[c]);
+  }
+}
+
+// binned |delta_k|^2 (grid_fft.cc:1133-1181): per-block shared histograms
+template <typename T>
+__global__ void k_pk(const cplx<T>* d, int n, double kfac, int nbins, double* acc) {
+  extern __shared__ double sh[];  // 4 * nbins
+  for (int b = threadIdx.x; b < 4 * nbins; b += blockDim.x) sh[b] = 0.0;
+  __syncthreads();
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  const double kmin = kfac, kmax = kfac * (n / 2), dk = kmin;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    const double kx = kcomp<double>(i, n, kfac), ky = kcomp<double>(j, n, kfac), kk = kcomp<double>(kz, n, kfac);
+    const double k = sqrt(kx * kx + ky * ky + kk * kk);
+    if (k >= kmin && k < kmax) {
+      const int b = (int)(k / dk);
+      const cplx<T> z = d[idx];
+      const double v = (double)z.x * (double)z.x + (double)z.y * (double)z.y;
+      const double w = (kz == 0) ? 1.0 : 2.0;
+      atomicAdd(&sh[b], w * v);
+      atomicAdd(&sh[nbins + b], w * v * v);
+      atomicAdd(&sh[2 * nbins + b], w * k);
+      atomicAdd(&sh[3 * nbins + b], w);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 4 * nbins; b += blockDim.x)
+    if (sh[b] != 0.0) atomicAdd(&acc[b], sh[b]);
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t pw_scale(T* d, size_t nreal, T x, cudaStream_t s) {
+  k_scale<T><<<grid_for(nreal, 4), kThreads, 0, s>>>(d, nreal, x);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pw_zero_dc(T* d, cudaStream_t s) {
+  k_zero_dc<T><<<1, 32, 0, s>>>(d);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pw_invlap(cplx<T>* d, int n, double kfac, cudaStream_t s) {
+  k_invlap<T><<<grid_for((size_t)n * n * (n / 2 + 1), 4), kThreads, 0, s>>>(d, n, T(kfac));
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pw_shift(cplx<T>* d, int n, double kfac, double dx, const double sh[3], cudaStream_t s) {
+  k_shift<T><<<grid_for((size_t)n * n * (n / 2 + 1), 4), kThreads, 0, s>>>(d, n, T(kfac), T(dx), T(sh[0]), T(sh[1]),
+                                                                          T(sh[2]));
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s) {
+  k_fill_from_f64<T><<<grid_for((size_t)n * n * n, 4), kThreads, 0, s>>>(d, src, n);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, double* acc, cudaStream_t s) {
+  const size_t smem = (size_t)4 * nbins * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_pk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_pk<T><<<grid_for((size_t)n * n * (n / 2 + 1), 8), kThreads, smem, s>>>(d, n, kfac, nbins, acc);
+  return cudaGetLastError();
+}
+
+#define INST(T)                                                                                      \
+  template cudaError_t pw_scale<T>(T*, size_t, T, cudaStream_t);                                     \
+  template cudaError_t pw_zero_dc<T>(T*, cudaStream_t);                                              \
+  template cudaError_t pw_invlap<T>(cplx<T>*, int, double, cudaStream_t);                            \
+  template cudaError_t pw_shift<T>(cplx<T>*, int, double, double, const double*, cudaStream_t);      \
+  template cudaError_t pw_fill_from_f64<T>(T*, const double*, int, cudaStream_t);                    \
+  template cudaError_t pw_power_spectrum<T>(const cplx<T>*, int, double, int, double*, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace mf

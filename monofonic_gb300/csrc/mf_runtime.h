@@ -1,0 +1,65 @@
+// Host-side objects behind the C ABI handles.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <string>
+
+#include "../../include/monofonic_gb300.h"
+#include "mf_internal.h"
+
+struct mf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  mf::TwiddleCache tw;
+  std::string err;
+};
+
+struct mf_grid {
+  mf_ctx* ctx = nullptr;
+  int n = 0;
+  double L = 0;
+  int prec = MF_PREC_F64;
+  int space = MF_SPACE_R;
+  void* d = nullptr;
+  size_t bytes = 0;
+};
+
+struct mf_conv {
+  mf_ctx* ctx = nullptr;
+  int n = 0;
+  double L = 0;
+  int prec = MF_PREC_F64;
+  int kind = MF_CONV_ORSZAG;
+  void* work = nullptr;   // nbuf * M*M*(n/2+1) complex
+  size_t work_bytes = 0;
+  int nbuf = 0;
+  mf_grid* fbuf = nullptr;  // N-grid intermediate of convolve3
+};
+
+namespace mf {
+
+int set_err(mf_ctx* c, int code, const std::string& msg);
+int cuda_err(mf_ctx* c, cudaError_t e, const char* where);
+
+inline size_t grid_reals(int n) { return (size_t)(n + 2) * n * n; }
+inline size_t prec_size(int prec) { return prec == MF_PREC_F32 ? 4 : 8; }
+
+// 3D transforms on an n-grid in the padded in-place layout (unitary)
+template <typename T> cudaError_t fft3d_r2c(mf_ctx* c, T* data, int n);
+template <typename T> cudaError_t fft3d_c2r(mf_ctx* c, T* data, int n);
+
+// convolution on k-space N-grids
+template <typename T>
+cudaError_t conv_run(mf_conv* cv, const Operand<T>* ops, int nop, cplx<T>* target, int out_op, T x,
+                     int post_invlap);
+
+// pointwise kernels (mf_pointwise.cu)
+template <typename T> cudaError_t pw_scale(T* d, size_t nreal, T x, cudaStream_t s);
+template <typename T> cudaError_t pw_zero_dc(T* d, cudaStream_t s);
+template <typename T> cudaError_t pw_invlap(cplx<T>* d, int n, double kfac, cudaStream_t s);
+template <typename T> cudaError_t pw_shift(cplx<T>* d, int n, double kfac, double dx, const double sh[3], cudaStream_t s);
+template <typename T> cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s);
+template <typename T>
+cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, double* acc /*4*nbins*/, cudaStream_t s);
+
+}  // namespace mf

@@ -1,0 +1,712 @@
+"""CPU oracle for the monofonIC nLPT field pipeline (test infrastructure only).
+
+This module is the checker, never the product: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
+it.  It restates, in numpy float64, the reference's own algorithm for the path
+white noise -> phi(1) -> Orszag-3/2 convolutions -> phi(2), phi(3), A(3) ->
+displacements, velocities, lattice positions and particle IDs.  Every function
+cites the reference file:line it follows (paths relative to the monofonIC
+source tree).
+
+Parity status: UNPINNED.  The reference ships no golden vectors, known-answer
+tests or fixtures for this path, and it cannot be compiled as shipped in this
+environment (it needs FFTW3, GSL, HDF5 and a CMake-generated
+``cmake_config.hh``).  Third-party arithmetic on the path is FFTW3 (unpinned
+version) for the transforms and GSL (unpinned) for the sigma_8 quadrature and
+cubic splines; this restatement uses numpy's pocketfft for the transforms
+(same sign and Hermitian-input conventions as FFTW's r2c/c2r, see ``c2r``) and
+scipy's QUADPACK for the sigma_8 integral.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# ----------------------------------------------------------------------------
+# physical constants  (include/physical_constants.hh:24-63)
+# ----------------------------------------------------------------------------
+_PI = 3.141592653589793115997963468544185161590576171875
+MPC_SI = 3.0857e22
+C_SI = 2.99792458e8
+G_SI = 6.6740800e-11
+KB_SI = 1.38064852e-23
+HBAR_SI = 1.054571800e-34
+SIGMA_SI = (_PI * _PI) * (KB_SI ** 4) / 60.0 / (HBAR_SI ** 3) / (C_SI * C_SI)
+RHOCRIT_H2_SI = 3 * 1e10 / (8 * _PI * G_SI) / MPC_SI / MPC_SI
+
+# default parameter set used for unspecified keys
+# (src/cosmology_parameters.cc:89-104, selected at include/cosmology_parameters.hh:87)
+_DEFAULTS = dict(h=0.67742, Omega_m=0.3099, Omega_b=0.048891054, Omega_DE=0.6901,
+                 w_0=-1.0, w_a=0.0, n_s=0.96822, A_s=2.1064e-9, k_p=0.05,
+                 YHe=0.245421, N_ur=2.046, m_nu1=0.06, m_nu2=0.0, m_nu3=0.0,
+                 Tcmb=2.7255)
+
+
+def cosmo_parameters(Omega_m, Omega_b, h, sigma_8, n_s, Omega_L=None, Tcmb=None,
+                     m_nu1=None, N_ur=None, zero_radiation=False, w_0=None, w_a=None):
+    """Derived cosmological parameters, ``ParameterSet = none`` branch.
+
+    Follows include/cosmology_parameters.hh:84-196 (reading with defaults,
+    derived radiation densities, flatness closure through Omega_DE).
+    """
+    d = _DEFAULTS
+    p = {}
+    p["Tcmb"] = d["Tcmb"] if Tcmb is None else Tcmb
+    p["h"] = h
+    p["n_s"] = n_s
+    p["sigma_8"] = sigma_8
+    p["A_s"] = -1.0
+    p["k_p"] = d["k_p"]
+    p["Omega_b"] = Omega_b
+    p["Omega_m"] = Omega_m
+    p["m_nu1"] = d["m_nu1"] if m_nu1 is None else m_nu1
+    p["m_nu2"] = d["m_nu2"]
+    p["m_nu3"] = d["m_nu3"]
+    n_nu_massive = int(p["m_nu1"] > 1e-9) + int(p["m_nu2"] > 1e-9) + int(p["m_nu3"] > 1e-9)
+    p["N_ur"] = (3.046 - n_nu_massive) if N_ur is None else N_ur
+    p["Omega_DE"] = d["Omega_DE"] if Omega_L is None else Omega_L
+    p["w_0"] = d["w_0"] if w_0 is None else w_0
+    p["w_a"] = d["w_a"] if w_a is None else w_a
+    p["H0"] = 100.0 * h
+    sum_m_nu = p["m_nu1"] + p["m_nu2"] + p["m_nu3"]
+    p["Omega_nu_massive"] = sum_m_nu / (93.14 * h * h)
+    p["Omega_gamma"] = (4 * SIGMA_SI / C_SI ** 3 * p["Tcmb"] ** 4.0
+                        / RHOCRIT_H2_SI / (h * h))
+    p["Omega_nu_massless"] = p["N_ur"] * p["Omega_gamma"] * 7. / 8. * (4. / 11.) ** (4. / 3.)
+    p["Omega_r"] = p["Omega_gamma"] + p["Omega_nu_massless"]
+    p["Omega_c"] = p["Omega_m"] - p["Omega_b"] - p["Omega_nu_massive"]
+    if zero_radiation:
+        p["Omega_r"] = 0.0
+    p["f_b"] = p["Omega_b"] / p["Omega_m"]
+    p["f_c"] = 1.0 - p["f_b"]
+    p["Omega_DE"] += 1.0 - p["Omega_m"] - p["Omega_DE"] - p["Omega_r"]
+    p["Omega_k"] = 0.0
+    return p
+
+
+# ----------------------------------------------------------------------------
+# Eisenstein & Hu (1998) fit  (src/plugins/transfer_eisenstein.cc:58-201)
+# ----------------------------------------------------------------------------
+class EisensteinHu:
+    """E&H 'full' transfer-function fit; restates TFset_parameters/TFfit_onek."""
+
+    def __init__(self, p):
+        # set_parameters (transfer_eisenstein.cc:186-194)
+        H0, Om, Ob, Tcmb = p["H0"], p["Omega_m"], p["Omega_b"], p["Tcmb"]
+        self.m_h0 = H0 * 0.01
+        self._set(Om * H0 * H0 * (0.01 * 0.01), Ob / Om, Tcmb)
+        self.fb = Ob / Om
+        self.fc = (Om - Ob) / Om
+
+    def _set(self, omhh, f_baryon, Tcmb):
+        # TFset_parameters (transfer_eisenstein.cc:58-122)
+        pw = math.pow
+        self.omhh = omhh
+        self.obhh = omhh * f_baryon
+        if Tcmb <= 0.0:
+            Tcmb = 2.728
+        th = Tcmb / 2.7
+        self.z_equality = 2.50e4 * omhh / th ** 4
+        self.k_equality = 0.0746 * omhh / th ** 2
+        b1 = 0.313 * pw(omhh, -0.419) * (1 + 0.607 * pw(omhh, 0.674))
+        b2 = 0.238 * pw(omhh, 0.223)
+        self.z_drag = (1291 * pw(omhh, 0.251) / (1 + 0.659 * pw(omhh, 0.828))
+                       * (1 + b1 * pw(self.obhh, b2)))
+        self.R_drag = 31.5 * self.obhh / th ** 4 * (1000 / (1 + self.z_drag))
+        self.R_equality = 31.5 * self.obhh / th ** 4 * (1000 / self.z_equality)
+        self.sound_horizon = (2. / 3. / self.k_equality * math.sqrt(6. / self.R_equality)
+                              * math.log((math.sqrt(1 + self.R_drag) + math.sqrt(self.R_drag + self.R_equality))
+                                         / (1 + math.sqrt(self.R_equality))))
+        self.k_silk = 1.6 * pw(self.obhh, 0.52) * pw(omhh, 0.73) * (1 + pw(10.4 * omhh, -0.95))
+        a1 = pw(46.9 * omhh, 0.670) * (1 + pw(32.1 * omhh, -0.532))
+        a2 = pw(12.0 * omhh, 0.424) * (1 + pw(45.0 * omhh, -0.582))
+        self.alpha_c = pw(a1, -f_baryon) * pw(a2, -f_baryon ** 3)
+        bb1 = 0.944 / (1 + pw(458 * omhh, -0.708))
+        bb2 = pw(0.395 * omhh, -0.0266)
+        self.beta_c = 1.0 / (1 + bb1 * (pw(1 - f_baryon, bb2) - 1))
+        y = self.z_equality / (1 + self.z_drag)
+        G = y * (-6. * math.sqrt(1 + y) + (2. + 3. * y) * math.log((math.sqrt(1 + y) + 1) / (math.sqrt(1 + y) - 1)))
+        self.alpha_b = 2.07 * self.k_equality * self.sound_horizon * pw(1 + self.R_drag, -0.75) * G
+        self.beta_node = 8.41 * pw(omhh, 0.435)
+        self.beta_b = 0.5 + f_baryon + (3. - 2. * f_baryon) * math.sqrt(pw(17.2 * omhh, 2.0) + 1)
+
+    def onek(self, k):
+        """TFfit_onek (transfer_eisenstein.cc:125-178), vectorised; returns (T_b, T_c)."""
+        k = np.abs(np.asarray(k, dtype=np.float64))
+        zero = k == 0.0
+        k = np.where(zero, 1.0, k)
+        q = k / 13.41 / self.k_equality
+        xx = k * self.sound_horizon
+        ln_beta = np.log(2.718282 + 1.8 * self.beta_c * q)
+        ln_nobeta = np.log(2.718282 + 1.8 * q)
+        C_alpha = 14.2 / self.alpha_c + 386.0 / (1 + 69.9 * q ** 1.08)
+        C_noalpha = 14.2 + 386.0 / (1 + 69.9 * q ** 1.08)
+        f = 1.0 / (1.0 + (xx / 5.4) ** 4)
+        T_c = (f * ln_beta / (ln_beta + C_noalpha * q * q)
+               + (1 - f) * ln_beta / (ln_beta + C_alpha * q * q))
+        s_tilde = self.sound_horizon * (1. + (self.beta_node / xx) ** 3) ** (-1. / 3.)
+        xt = k * s_tilde
+        T_b_T0 = ln_nobeta / (ln_nobeta + C_noalpha * q * q)
+        T_b = np.sin(xt) / xt * (T_b_T0 / (1. + (xx / 5.2) ** 2)
+                                 + self.alpha_b / (1. + (self.beta_b / xx) ** 3)
+                                 * np.exp(-(k / self.k_silk) ** 1.4))
+        T_b = np.where(zero, 1.0, T_b)
+        T_c = np.where(zero, 1.0, T_c)
+        return T_b, T_c
+
+    def at_k(self, k):
+        """at_k (transfer_eisenstein.cc:196-201): k in h/Mpc."""
+        tb, tc = self.onek(np.asarray(k, dtype=np.float64) * self.m_h0)
+        return self.fb * tb + self.fc * tc
+
+
+# ----------------------------------------------------------------------------
+# growth factor and normalisation (include/cosmology_calculator.hh:91-463)
+# ----------------------------------------------------------------------------
+def _H_of_a(p, a):
+    # cosmology_calculator.hh:317-325
+    HH2 = (p["Omega_r"] / (a * a * a * a) + p["Omega_m"] / (a * a * a) + p["Omega_k"] / (a * a)
+           + p["Omega_DE"] * a ** (-3. * (1. + p["w_0"] + p["w_a"])) * math.exp(-3. * (1.0 - a) * p["w_a"]))
+    return p["H0"] * math.sqrt(HH2)
+
+
+_CK = dict(a2=0.20, a3=0.30, a4=0.60, a5=1.0, a6=0.8750,
+           b21=0.20, b31=3.0 / 40.0, b32=9.0 / 40.0, b41=0.30, b42=-0.90, b43=1.20,
+           b51=-11.0 / 54.0, b52=2.50, b53=-70.0 / 27.0, b54=35.0 / 27.0,
+           b61=1631.0 / 55296.0, b62=175.0 / 512.0, b63=575.0 / 13824.0, b64=44275.0 / 110592.0,
+           b65=253.0 / 4096.0, c1=37.0 / 378.0, c3=250.0 / 621.0, c4=125.0 / 594.0, c6=512.0 / 1771.0)
+_CK["dc1"] = _CK["c1"] - 2825.0 / 27648.0
+_CK["dc3"] = _CK["c3"] - 18575.0 / 48384.0
+_CK["dc4"] = _CK["c4"] - 13525.0 / 55296.0
+_CK["dc5"] = -277.0 / 14336.0
+_CK["dc6"] = _CK["c6"] - 0.250
+
+
+def _growth_table(p):
+    """compute_growth (cosmology_calculator.hh:91-151) with the Cash-Karp
+    quality-controlled stepper of include/math/ode_integrate.hh:39-111."""
+    Om, H0 = p["Omega_m"], p["H0"]
+
+    def rhs(y):
+        a, D, Dp = y
+        Ha = _H_of_a(p, a)
+        return np.array([a * a * Ha, Dp, -a * Ha * Dp + 1.5 * Om * H0 ** 2 * D / a])
+
+    a0 = 1e-10
+    y = np.array([a0, a0, 2.0 * a0 * _H_of_a(p, a0) / C_SI ** 2])
+    t = 1.0 / (a0 * _H_of_a(p, a0))
+    dt = 1e-9
+    eps = 1e-10
+    c = _CK
+    ta, tD, tf = [], [], []
+    while y[0] < 2.0:
+        yscale = np.abs(y) + dt * np.abs(rhs(y))
+        h = dt
+        while True:
+            k1 = h * rhs(y)
+            k2 = h * rhs(y + c["b21"] * k1)
+            k3 = h * rhs(y + c["b31"] * k1 + c["b32"] * k2)
+            k4 = h * rhs(y + c["b41"] * k1 + c["b42"] * k2 + c["b43"] * k3)
+            k5 = h * rhs(y + c["b51"] * k1 + c["b52"] * k2 + c["b53"] * k3 + c["b54"] * k4)
+            k6 = h * rhs(y + c["b61"] * k1 + c["b62"] * k2 + c["b63"] * k3 + c["b64"] * k4 + c["b65"] * k5)
+            ytmp = y + c["c1"] * k1 + c["c3"] * k3 + c["c4"] * k4 + c["c6"] * k6
+            yerr = c["dc1"] * k1 + c["dc3"] * k3 + c["dc4"] * k4 + c["dc5"] * k5 + c["dc6"] * k6
+            errmax = float(np.max(np.abs(yerr / yscale))) / eps
+            if errmax > 1.0:
+                h *= max(0.1, 0.9 * errmax ** -0.25)
+                continue
+            hnext = h * 0.9 * errmax ** -0.2 if errmax > 1.89e-4 else 5 * h
+            t += h
+            y = ytmp
+            break
+        ta.append(y[0]); tD.append(y[1]); tf.append(y[2])
+        dt = hnext
+    ta = np.array(ta); tD = np.array(tD); tf = np.array(tf)
+    tf = tf / (ta * np.array([_H_of_a(p, a) for a in ta]) * tD)
+    return ta, tD, tf
+
+
+class _LogLogSpline:
+    """interpolated_function_1d<true,true,false> (include/math/interpolate.hh:29-103):
+    natural cubic spline of log(y) against log(x) (GSL cspline)."""
+
+    def __init__(self, x, y):
+        from scipy.interpolate import CubicSpline
+        self.s = CubicSpline(np.log(x), np.log(y), bc_type="natural")
+
+    def __call__(self, x):
+        return float(np.exp(self.s(math.log(x))))
+
+
+@dataclass
+class CosmoScalars:
+    """Host scalars that cross the boundary: D+(a_start), vfac, sqrt(pnorm)."""
+    Dplus: float
+    vfac: float
+    pnorm: float
+    n_s: float
+    params: dict = field(default_factory=dict)
+
+
+def cosmo_calculator(p, zstart):
+    """cosmology::calculator ctor (cosmology_calculator.hh:166-210) plus
+    get_growth_factor/get_vfact (:334-363) and compute_pnorm_from_sigma8 (:439-463)."""
+    from scipy.integrate import quad
+    ta, tD, tf = _growth_table(p)
+    D_of_a = _LogLogSpline(ta, tD)
+    f_of_a = _LogLogSpline(ta, tf)
+    Dnow = D_of_a(1.0)
+    astart = 1.0 / (1.0 + zstart)
+    Dplus = D_of_a(astart) / Dnow
+    vfac = f_of_a(astart) * astart * _H_of_a(p, astart) / p["h"]
+    eh = EisensteinHu(p)
+    ns = p["n_s"]
+
+    def dsigma8(k):  # dSigma8 (cosmology_calculator.hh:368-380)
+        x = k * 8.0
+        w = 1.0 - 0.1 * x * x if x < 0.001 else 3.0 * (math.sin(x) - x * math.cos(x)) / (x * x * x)
+        tfk = float(eh.at_k(k))
+        return k * k * w * w * k ** ns * tfk * tfk
+
+    # GSL QAG-61 to rel 1e-10 over [kmin, kmax] = [1e-4, 1e4]
+    # (cosmology_calculator.hh:62-83, 439-452); QUADPACK over log-spaced pieces here
+    edges = np.logspace(-4, 4, 161)
+    sig = sum(quad(dsigma8, a, b, epsabs=0, epsrel=1e-13, limit=200)[0]
+              for a, b in zip(edges[:-1], edges[1:]))
+    sigma8_meas = math.sqrt(4.0 * math.pi * sig)
+    pnorm = p["sigma_8"] ** 2 / sigma8_meas ** 2
+    return CosmoScalars(Dplus=Dplus, vfac=vfac, pnorm=pnorm, n_s=ns, params=p)
+
+
+# ----------------------------------------------------------------------------
+# white noise: project RNG plugin (Philox4x32-10 + Box-Muller), keyed by cell
+# ----------------------------------------------------------------------------
+_M0, _M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+_W0, _W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
+_MASK = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32(ctr, key):
+    """Philox4x32-10 (Salmon et al. 2011), vectorised on uint64 lanes."""
+    c0, c1, c2, c3 = (np.asarray(c, dtype=np.uint64) & _MASK for c in ctr)
+    k0, k1 = np.uint64(key[0]) & _MASK, np.uint64(key[1]) & _MASK
+    for _ in range(10):
+        p0 = _M0 * c0
+        p1 = _M1 * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & _MASK
+        hi1, lo1 = p1 >> np.uint64(32), p1 & _MASK
+        c0, c1, c2, c3 = (hi1 ^ c1 ^ k0) & _MASK, lo1, (hi0 ^ c3 ^ k1) & _MASK, lo0
+        k0 = (k0 + _W0) & _MASK
+        k1 = (k1 + _W1) & _MASK
+    return c0, c1, c2, c3
+
+
+def white_noise(n, seed):
+    """Real-space i.i.d. N(0,1) float64 noise on an n^3 grid.
+
+    Cell c = (i*n + j)*n + k takes draw c of a stream in which pair
+    p = c // 2 is one Philox4x32-10 block at counter (p_lo, p_hi, 0, 0) and key
+    (seed_lo, seed_hi); two 53-bit uniforms u1, u2 in (0,1) go through
+    Box-Muller: cell 2p gets r cos(2 pi u2), cell 2p+1 gets r sin(2 pi u2).
+    This plays the role of RNG_plugin::Fill_Grid (include/random_plugin.hh:37).
+    """
+    ncell = n * n * n
+    npair = (ncell + 1) // 2
+    p = np.arange(npair, dtype=np.uint64)
+    x0, x1, x2, x3 = philox4x32((p & _MASK, p >> np.uint64(32), 0 * p, 0 * p),
+                                (seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF))
+    b1 = (x0 | (x1 << np.uint64(32))) >> np.uint64(11)
+    b2 = (x2 | (x3 << np.uint64(32))) >> np.uint64(11)
+    u1 = (b1.astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+    u2 = (b2.astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+    r = np.sqrt(-2.0 * np.log(u1))
+    th = 2.0 * math.pi * u2
+    out = np.empty(2 * npair)
+    out[0::2] = r * np.cos(th)
+    out[1::2] = r * np.sin(th)
+    return out[:ncell].reshape(n, n, n)
+
+
+# ----------------------------------------------------------------------------
+# Grid_FFT essentials (include/grid_fft.hh, src/grid_fft.cc)
+# ----------------------------------------------------------------------------
+def r2c(x):
+    """FourierTransformForward + ApplyNorm (grid_fft.cc:199-235): FFTW r2c
+    (sign -1) of an n^3 real array, scaled by 1/sqrt(n^3)."""
+    n = x.shape[0]
+    return np.fft.rfftn(x, axes=(0, 1, 2)) / math.sqrt(float(n) ** 3)
+
+
+def c2r(X, n=None):
+    """FourierTransformBackward + ApplyNorm (grid_fft.cc:238-270): FFTW c2r
+    (sign +1) scaled by 1/sqrt(n^3).  For spectra that are not Hermitian on the
+    kz = 0 and kz = n/2 planes the result is that of complex inverse
+    transforms along x and y followed by a c2r along z that ignores the
+    imaginary parts of the kz = 0 and kz = n/2 terms -- FFTW's convention,
+    and numpy's irfftn."""
+    if n is None:
+        n = X.shape[0]
+    return np.fft.irfftn(X, s=(n, n, n), axes=(0, 1, 2)) * (float(n) ** 3 / math.sqrt(float(n) ** 3))
+
+
+def kvec_1d(n, L):
+    """get_k per axis (grid_fft.hh:281-296): (i - n*[i > n/2]) * 2pi/L (Nyquist stays +)."""
+    i = np.arange(n, dtype=np.float64)
+    return (i - (i > n // 2) * n) * (2.0 * math.pi / L)
+
+
+def grad_1d(n, L):
+    """gradient factor (grid_fft.hh:376-385, operators.hh:49-55): real part of
+    i*k per axis, zero at the Nyquist index."""
+    g = kvec_1d(n, L)
+    g[n // 2] = 0.0
+    return g
+
+
+def kgrids(n, L):
+    k1 = kvec_1d(n, L)
+    kz = k1[: n // 2 + 1]
+    return k1[:, None, None], k1[None, :, None], kz[None, None, :]
+
+
+def ggrids(n, L):
+    g1 = grad_1d(n, L)
+    gz = g1[: n // 2 + 1]
+    return [g1[:, None, None], g1[None, :, None], gz[None, None, :]]
+
+
+def hessian(F, L, a, b):
+    """kfunc of BaseConvolver::convolve_Hessians (convolution.hh:137-160):
+    (i g_a)(i g_b) F = -g_a g_b F."""
+    n = F.shape[0]
+    g = ggrids(n, L)
+    return -(g[a] * g[b]) * F
+
+
+def sum_hessian(F, L, d1, d2, sign=+1):
+    """kfunc of convolve_SumOfHessians / DifferenceOfHessians (convolution.hh:214-274)."""
+    n = F.shape[0]
+    g = ggrids(n, L)
+    return (-(g[d1[0]] * g[d1[1]]) + sign * -(g[d2[0]] * g[d2[1]])) * F
+
+
+# ----------------------------------------------------------------------------
+# Orszag 3/2 convolver (include/convolution.hh:429-669)
+# ----------------------------------------------------------------------------
+def pad_insert(Fk, N):
+    """OrszagConvolver::pad_insert (convolution.hh:570-592)."""
+    M = 3 * N // 2
+    fp = np.zeros((M, M, M // 2 + 1), dtype=np.complex128)
+    rfac = math.pow(1.5, 1.5)
+    ip = np.arange(N)
+    ip = np.where(ip > N // 2, ip + N // 2, ip)
+    fp[np.ix_(ip, ip, np.arange(N // 2 + 1))] = Fk * rfac
+    return fp
+
+
+def unpad(Fp, N):
+    """OrszagConvolver::unpad (convolution.hh:618-653): gather, divide by
+    sqrt(M^3)/sqrt(N^3), zero every i, j or k == N/2 plane."""
+    M = Fp.shape[0]
+    rfac = math.sqrt(float(M * M * M)) / math.sqrt(float(N * N * N))
+    ip = np.arange(N)
+    ip = np.where(ip > N // 2, ip + N // 2, ip)
+    out = Fp[np.ix_(ip, ip, np.arange(N // 2 + 1))] / rfac
+    out[N // 2, :, :] = 0
+    out[:, N // 2, :] = 0
+    out[:, :, N // 2] = 0
+    return out
+
+
+def orszag_conv2(A, B):
+    """OrszagConvolver::convolve2 (convolution.hh:513-535) on pre-evaluated
+    kfunc arrays A, B (N-grid half spectra); returns the unpadded result."""
+    N = A.shape[0]
+    M = 3 * N // 2
+    f1 = c2r(pad_insert(A, N), M)
+    f2 = c2r(pad_insert(B, N), M)
+    return unpad(r2c(f2 * f1), N)
+
+
+def orszag_conv3(A, B, C):
+    """OrszagConvolver::convolve3 (convolution.hh:543-549): two chained
+    convolve2, the intermediate truncated and Nyquist-zeroed."""
+    return orszag_conv2(orszag_conv2(A, B), C)
+
+
+def naive_conv2(A, B):
+    """NaiveConvolver::convolve2 (convolution.hh:328-356)."""
+    N = A.shape[0]
+    return r2c(c2r(B, N) * c2r(A, N))
+
+
+def naive_conv3(A, B, C):
+    """NaiveConvolver::convolve3 (convolution.hh:359-402)."""
+    N = A.shape[0]
+    return r2c(c2r(B, N) * c2r(A, N) * c2r(C, N))
+
+
+# output operators (include/operators.hh:25-35), applied per real scalar;
+# elementwise on complex arrays they are the same arithmetic
+def op_apply(target, value, kind, x=1.0):
+    if kind == "assign":
+        target[...] = value
+    elif kind == "add":
+        target += value
+    elif kind == "sub":
+        target -= value
+    elif kind == "axpy":
+        target += value * x
+    else:
+        raise ValueError(kind)
+
+
+def inverse_laplacian(F, L):
+    """apply_InverseLaplacian (grid_fft.hh:440-449): -x/k^2 then zero_DC_mode."""
+    n = F.shape[0]
+    kx, ky, kz = kgrids(n, L)
+    k2 = kx * kx + ky * ky + kz * kz
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = -F / k2
+    out[0, 0, 0] = 0
+    return out
+
+
+# ----------------------------------------------------------------------------
+# IC generator LPT section (src/ic_generator.cc:209-563)
+# ----------------------------------------------------------------------------
+@dataclass
+class LPTFields:
+    phi: np.ndarray
+    phi2: np.ndarray | None
+    phi3: np.ndarray | None
+    A3: list | None
+
+
+def amplitude(kmod, cs, eh):
+    """get_amplitude (cosmology_calculator.hh:405-408)."""
+    return np.power(kmod, 0.5 * cs.n_s) * eh.at_k(kmod) * math.sqrt(cs.pnorm)
+
+
+def lpt_potentials(noise_r, L, order, cs, eh=None, convolver="orszag", fixing=False, inversion=False):
+    """ic_generator::run, LPT part (ic_generator.cc:249-563 without fNL/tides).
+
+    Returns the growth-scaled potentials phi*g1, phi2*g2, phi3*g3, A3*g3c in
+    k-space (n x n x n/2+1 complex each).
+    """
+    if eh is None:
+        eh = EisensteinHu(cs.params)
+    conv2 = orszag_conv2 if convolver == "orszag" else naive_conv2
+    conv3 = orszag_conv3 if convolver == "orszag" else naive_conv3
+    n = noise_r.shape[0]
+    volfac = math.pow(L / n / 2.0 / math.pi, 1.5)
+    D = cs.Dplus
+    g1 = -D
+    g2 = -3.0 / 7.0 * D * D if order > 1 else 0.0
+    g3 = 1.0 / 3.0 * D * D * D if order > 2 else 0.0
+    g3c = 1.0 / 7.0 * D * D * D if order > 2 else 0.0
+
+    wn = r2c(noise_r)
+    # normalise (ic_generator.cc:341-346)
+    if fixing:
+        a = np.abs(wn)
+        wn = np.where(a != 0.0, wn / np.where(a != 0, a, 1.0), wn)
+    wn = (-1.0 if inversion else 1.0) * wn / volfac
+    # phi(1) (ic_generator.cc:449-457)
+    kx, ky, kz = kgrids(n, L)
+    kmod = np.sqrt(kx * kx + ky * ky + kz * kz)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        phi = -(wn * amplitude(kmod, cs, eh)) / (kmod * kmod)
+    phi[0, 0, 0] = 0
+
+    H = lambda F, a, b: hessian(F, L, a, b)
+    phi2 = phi3 = A3 = None
+    if order > 1:
+        # ic_generator.cc:471-475
+        s = conv2(H(phi, 0, 0), sum_hessian(phi, L, (1, 1), (2, 2)))
+        s = s + conv2(H(phi, 1, 1), H(phi, 2, 2))
+        s = s - conv2(H(phi, 0, 1), H(phi, 0, 1))
+        s = s - conv2(H(phi, 0, 2), H(phi, 0, 2))
+        s = s - conv2(H(phi, 1, 2), H(phi, 1, 2))
+        phi2 = inverse_laplacian(s, L)
+    if order > 2:
+        # 3a (ic_generator.cc:511-515)
+        t = conv3(H(phi, 0, 0), H(phi, 1, 1), H(phi, 2, 2))
+        t = t + conv3(H(phi, 0, 1), H(phi, 0, 2), H(phi, 1, 2)) * 2.0
+        t = t - conv3(H(phi, 1, 2), H(phi, 1, 2), H(phi, 0, 0))
+        t = t - conv3(H(phi, 0, 2), H(phi, 0, 2), H(phi, 1, 1))
+        t = t - conv3(H(phi, 0, 1), H(phi, 0, 1), H(phi, 2, 2))
+        # 3b (ic_generator.cc:522-527)
+        t = t + conv2(H(phi, 0, 0), sum_hessian(phi2, L, (1, 1), (2, 2))) * (-5.0 / 7.0)
+        t = t + conv2(H(phi, 1, 1), sum_hessian(phi2, L, (2, 2), (0, 0))) * (-5.0 / 7.0)
+        t = t + conv2(H(phi, 2, 2), sum_hessian(phi2, L, (0, 0), (1, 1))) * (-5.0 / 7.0)
+        t = t + conv2(H(phi, 0, 1), H(phi2, 0, 1)) * (+10.0 / 7.0)
+        t = t + conv2(H(phi, 0, 2), H(phi2, 0, 2)) * (+10.0 / 7.0)
+        t = t + conv2(H(phi, 1, 2), H(phi2, 1, 2)) * (+10.0 / 7.0)
+        phi3 = inverse_laplacian(t, L)
+        # A(3) (ic_generator.cc:534-545)
+        A3 = []
+        for d in range(3):
+            dp, dpp = (d + 1) % 3, (d + 2) % 3
+            a = conv2(H(phi2, d, dp), H(phi, d, dpp))
+            a = a - conv2(H(phi2, d, dpp), H(phi, d, dp))
+            a = a + conv2(H(phi, dp, dpp), sum_hessian(phi2, L, (dp, dp), (dpp, dpp), sign=-1))
+            a = a - conv2(H(phi2, dp, dpp), sum_hessian(phi, L, (dp, dp), (dpp, dpp), sign=-1))
+            A3.append(inverse_laplacian(a, L))
+    # growth scaling (ic_generator.cc:550-563)
+    phi = phi * g1
+    if order > 1:
+        phi2 = phi2 * g2
+    if order > 2:
+        phi3 = phi3 * g3
+        A3 = [a * g3c for a in A3]
+    return LPTFields(phi, phi2, phi3, A3)
+
+
+# ----------------------------------------------------------------------------
+# displacement / velocity assembly and the particle lattice
+# (src/ic_generator.cc:794-948, include/particle_generator.hh)
+# ----------------------------------------------------------------------------
+LATTICE_SHIFTS = {  # particle_generator.hh:47-54
+    0: [(0.0, 0.0, 0.0)],
+    1: [(0.0, 0.0, 0.0), (0.5, 0.5, 0.5)],
+    2: [(0.0, 0.0, 0.0), (0.0, 0.5, 0.5), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0)],
+    3: [(0.0, 0.0, 0.0), (0.0, 0.0, 0.5), (0.0, 0.5, 0.0), (0.0, 0.5, 0.5),
+        (0.5, 0.0, 0.0), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0), (0.5, 0.5, 0.5)],
+}
+
+
+def displacement_k(f: LPTFields, L, d, order, unit=1.0, vel=False, vfac=0.0, vcorr=None):
+    """k-space combination of ic_generator.cc:829-858 (positions) or
+    :884-931 (velocities), times unit/L, DC zeroed, with the fourier_gradient
+    operator of operators.hh:38-61 (or a PLT gradient passed as ``vcorr``)."""
+    n = f.phi.shape[0]
+    g = ggrids(n, L)
+    dp, dpp = (d + 1) % 3, (d + 2) % 3
+    if not vel:
+        tot = f.phi.copy()
+        if order > 1:
+            tot = tot + f.phi2
+        if order > 2:
+            tot = tot + f.phi3
+        t = (1j * g[d]) * tot
+        if order > 2:
+            t = t + ((1j * g[dp]) * f.A3[dpp] - (1j * g[dpp]) * f.A3[dp])
+    else:
+        tot = vfac * f.phi
+        if order > 1:
+            tot = tot + 2 * vfac * f.phi2
+        if order > 2:
+            tot = tot + 3 * vfac * f.phi3
+        t = (1j * g[d]) * tot
+        if order > 2:
+            t = t + 3 * vfac * ((1j * g[dp]) * f.A3[dpp] - (1j * g[dpp]) * f.A3[dp])
+        if vcorr is not None:
+            t = t * vcorr
+    t = t * (unit / L)
+    t[0, 0, 0] = 0
+    return t
+
+
+def shift_field(fr, s, L):
+    """shift_field (grid_fft.hh:832-842): r2c, times exp(i s.k dx), c2r."""
+    n = fr.shape[0]
+    F = r2c(fr)
+    kx, ky, kz = kgrids(n, L)
+    dx = L / n
+    F = F * np.exp(1j * (s[0] * kx * dx + s[1] * ky * dx + s[2] * kz * dx))
+    return c2r(F, n)
+
+
+def lattice_positions_component(field_r, d, lattice, unit, L):
+    """set_positions, Bravais branch (particle_generator.hh:499-544), one
+    component d: returns the overload*n^3 values pos[ip] in particle order
+    ishift*n^3 + cell."""
+    n = field_r.shape[0]
+    shifts = LATTICE_SHIFTS[lattice]
+    out = []
+    fr = field_r
+    idx = np.arange(n, dtype=np.float64)
+    for ish, s in enumerate(shifts):
+        if ish > 0:
+            prev = shifts[ish - 1]
+            fr = shift_field(fr, tuple(s[a] - prev[a] for a in range(3)), L)
+        q = (idx + s[d]) / float(n)
+        qg = [q[:, None, None], q[None, :, None], q[None, None, :]][d]
+        out.append((qg * unit + fr).reshape(-1))
+    return np.concatenate(out)
+
+
+def lattice_velocities_component(field_r, lattice, L):
+    """set_velocities, Bravais branch (particle_generator.hh:597-639)."""
+    shifts = LATTICE_SHIFTS[lattice]
+    out = []
+    fr = field_r
+    for ish, s in enumerate(shifts):
+        if ish > 0:
+            prev = shifts[ish - 1]
+            fr = shift_field(fr, tuple(s[a] - prev[a] for a in range(3)), L)
+        out.append(fr.reshape(-1))
+    return np.concatenate(out)
+
+
+def particle_ids(n, lattice, id_offset=0):
+    """lattice_generator ctor, Bravais branch (particle_generator.hh:212-253):
+    particle ipcount + iload*n^3 gets id offset*overload*n^3 + overload*cell + iload."""
+    overload = 1 << max(0, lattice)
+    ncell = n * n * n
+    cell = np.arange(ncell, dtype=np.uint64)
+    off = np.uint64(id_offset * overload * ncell)
+    ids = np.empty(overload * ncell, dtype=np.uint64)
+    for il in range(overload):
+        ids[il * ncell:(il + 1) * ncell] = off + np.uint64(overload) * cell + np.uint64(il)
+    return ids
+
+
+def particles(f: LPTFields, L, order, vfac, lattice=0, lunit=1.0, vunit=1.0):
+    """Positions (AoS [ip][3]), velocities (AoS) and ids for the Lagrangian
+    particle output of ic_generator.cc:794-948."""
+    n = f.phi.shape[0]
+    overload = 1 << max(0, lattice)
+    pos = np.empty((overload * n ** 3, 3))
+    vel = np.empty((overload * n ** 3, 3))
+    for d in range(3):
+        fr = c2r(displacement_k(f, L, d, order, unit=lunit), n)
+        pos[:, d] = lattice_positions_component(fr, d, lattice, lunit, L)
+    for d in range(3):
+        fr = c2r(displacement_k(f, L, d, order, unit=vunit, vel=True, vfac=vfac), n)
+        vel[:, d] = lattice_velocities_component(fr, lattice, L)
+    return pos, vel, particle_ids(n, lattice)
+
+
+# ----------------------------------------------------------------------------
+# power spectrum (src/grid_fft.cc:1133-1210)
+# ----------------------------------------------------------------------------
+def power_spectrum(F, L):
+    """Compute_PowerSpectrum of a k-space field; returns (k, P, eP, count)."""
+    n = F.shape[0]
+    kfac = 2.0 * math.pi / L
+    kmax = kfac * (n // 2)
+    kmin = kfac
+    nbins = int(kmax / kmin)
+    kx, ky, kz = kgrids(n, L)
+    k = np.sqrt(kx * kx + ky * ky + kz * kz)
+    k = np.broadcast_to(k, F.shape)
+    v = F.real ** 2 + F.imag ** 2
+    w = np.ones(F.shape)
+    w[:, :, 1:] = 2.0
+    sel = (k >= kmin) & (k < kmax)
+    idx = (k[sel] / kmin).astype(np.int64)
+    bk = np.bincount(idx, weights=(w * k)[sel], minlength=nbins)[:nbins]
+    bP = np.bincount(idx, weights=(w * v)[sel], minlength=nbins)[:nbins]
+    beP = np.bincount(idx, weights=(w * v * v)[sel], minlength=nbins)[:nbins]
+    bc = np.bincount(idx, weights=w[sel], minlength=nbins)[:nbins]
+    volfac = L ** 3 / (2.0 * math.pi) ** 3
+    fftfac = 1.0 / float(n) ** 3
+    with np.errstate(divide="ignore", invalid="ignore"):
+        bk = np.where(bc > 0, bk / bc, 0)
+        bP = np.where(bc > 0, bP / bc * volfac * fftfac, 0)
+        beP = np.where(bc > 0, np.sqrt(beP / bc - bP * bP) / np.sqrt(bc) * volfac * fftfac, 0)
+    return bk, bP, beP, bc.astype(np.int64)
