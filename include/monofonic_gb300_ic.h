@@ -1,0 +1,123 @@
+/*
+ * monofonic_gb300_ic.h -- C ABI of the initial-condition level of libmfgpu:
+ * host cosmology scalars, the white-noise plugin, the LPT pipeline of
+ * ic_generator::run and particle/field assembly.
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the monofonIC source tree).  Status codes are those of
+ * monofonic_gb300.h.
+ */
+#ifndef MONOFONIC_GB300_IC_H
+#define MONOFONIC_GB300_IC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "monofonic_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- cosmology (include/cosmology_parameters.hh:84-196,
+ *      include/cosmology_calculator.hh:166-463) ---------------------------- */
+typedef struct {
+  double Omega_m, Omega_b, h, sigma_8, n_s;
+  double Omega_L;    /* < 0: default set (Planck2018EE+BAO+SN) value      */
+  double Tcmb;       /* <= 0: 2.7255                                       */
+  double m_nu1;      /* < 0: 0.06 eV                                       */
+  double N_ur;       /* < 0: 3.046 - number of massive species             */
+  double w_0, w_a;   /* dark energy, -1 and 0 for a cosmological constant */
+  int zero_radiation;
+} mf_cosmo_params;
+
+typedef struct {
+  double Dplus;      /* get_growth_factor(a_start)          (:334-337) */
+  double vfac;       /* get_vfact(a_start)                  (:360-363) */
+  double f;          /* dlog D+ / dlog a at a_start                    */
+  double pnorm;      /* (sigma_8 / sigma_8,measured)^2      (:458-463) */
+  double sigma8_measured;
+  double n_s, h, H0, Omega_m, Omega_b, Omega_r, Omega_DE, Tcmb;
+} mf_cosmo_scalars;
+
+/* fill *p with the documented defaults for unset keys */
+void mf_cosmo_params_default(mf_cosmo_params* p);
+/* cosmology::calculator ctor + scalars at z_start */
+int mf_cosmology_compute(const mf_cosmo_params* p, double zstart, mf_cosmo_scalars* out);
+/* TransferFunction_plugin::compute(k, delta_matter) of the eisenstein plugin
+ * (src/plugins/transfer_eisenstein.cc:238-242), k in h/Mpc, n values */
+int mf_eh_transfer(const mf_cosmo_params* p, const double* k, double* out, size_t n);
+
+/* ---- white noise: RNG plugin (include/random_plugin.hh:26-39) ----------- */
+/* i.i.d. N(0,1) float64 on an n^3 grid, cell (i*n+j)*n+k; Philox4x32-10 block
+ * p = cell/2 at counter (p_lo, p_hi, 0, 0), key (seed_lo, seed_hi), two
+ * 53-bit uniforms through Box-Muller (cos -> even cell, sin -> odd cell).
+ * Host, multithreaded (nthreads <= 0: all hardware threads). */
+int mf_white_noise_host(int n, uint64_t seed, double* out, int nthreads);
+
+/* ---- LPT pipeline (src/ic_generator.cc:90-948) -------------------------- */
+enum { MF_OUT_PARTICLES = 0, MF_OUT_FIELDS = 1 };
+enum { MF_LOC_HOST = 0, MF_LOC_DEVICE = 1 };
+
+typedef struct {
+  int ngrid;          /* setup/GridRes                                     */
+  double boxlen;      /* setup/BoxLength [Mpc/h]                           */
+  double zstart;      /* setup/zstart                                      */
+  int lpt_order;      /* setup/LPTorder, 1..3                              */
+  int lattice;        /* setup/ParticleLoad, MF_LATTICE_*                  */
+  int precision;      /* MF_PREC_F64 plain or MF_PREC_F32 bulk             */
+  int convolver;      /* MF_CONV_ORSZAG or MF_CONV_NAIVE                   */
+  int fixing;         /* setup/DoFixing                                    */
+  int inversion;      /* setup/DoInversion                                 */
+  int plt;            /* PLT corrected gradient and growth rate (ENABLE_PLT) */
+  mf_cosmo_scalars cosmo; /* D+, vfac, pnorm, n_s, h, Omega_m, Omega_b, Tcmb */
+  const double* tk_table; /* optional host table T(k) at k = sqrt(k2)*2pi/L,
+                             k2 = 0..3(n/2)^2; NULL: device Eisenstein-Hu   */
+  double lunit, vunit;    /* output_plugin::position_unit / velocity_unit   */
+  int out_kind;           /* MF_OUT_PARTICLES or MF_OUT_FIELDS              */
+  int pos64;              /* output_plugin::has_64bit_reals                 */
+  int id64;               /* output_plugin::has_64bit_ids                   */
+} mf_ic_params;
+
+/* Particle container (include/particle_container.hh:29-139): positions and
+ * velocities AoS [npart][3] in float or double, ids u32 or u64, particle
+ * ip = ishift*n^3 + cell.  For MF_OUT_FIELDS, pos and vel each hold three
+ * n^3 float64 grids (dx,dy,dz / vx,vy,vz, row-major i,j,k) and ids is unused. */
+typedef struct {
+  void* pos;
+  void* vel;
+  void* ids;
+  int64_t npart;
+  int location;       /* MF_LOC_HOST or MF_LOC_DEVICE */
+} mf_particles;
+
+/* number of particles and output bytes for a parameter set */
+int mf_ic_output_size(const mf_ic_params* p, int64_t* npart, size_t* pos_bytes, size_t* vel_bytes,
+                      size_t* id_bytes);
+/* device bytes the pipeline needs (fields, convolution buffers, particles) */
+int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes);
+
+typedef struct mf_ic mf_ic;
+/* allocate the pipeline's device state for a parameter set */
+int mf_ic_create(mf_ctx* ctx, const mf_ic_params* p, mf_ic** out);
+int mf_ic_destroy(mf_ic* ic);
+/* upload the real-space white noise (n^3 float64, host or device pointer) */
+int mf_ic_set_noise(mf_ic* ic, const double* noise, int location);
+/* run noise -> phi(1..3), A(3) -> particles or fields into out (device
+ * buffers of the ic when out->location is MF_LOC_DEVICE and out->pos is
+ * NULL; copies to host buffers when MF_LOC_HOST) */
+int mf_ic_run(mf_ic* ic, mf_particles* out);
+/* per-stage device times of the last run in milliseconds:
+ * [noise r2c + phi1, phi2, phi3, A3, positions, velocities, ids, d2h] */
+int mf_ic_stage_times(const mf_ic* ic, double* ms8);
+/* access to the potentials of the last run (k-space grids, unscaled, i.e.
+ * before the growth factors of ic_generator.cc:550-563): which = 0 phi,
+ * 1 phi2, 2 phi3, 3..5 A3x..z */
+int mf_ic_get_potential(mf_ic* ic, int which, mf_grid** out);
+/* Grid of the k-space white noise after normalisation (ic_generator.cc:341-346) */
+int mf_ic_get_noise(mf_ic* ic, mf_grid** out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MONOFONIC_GB300_IC_H */

@@ -61,6 +61,53 @@ SIGNATURES = {
                                     C.POINTER(mf_operand), C.c_void_p, C.c_int, C.c_double]),
 }
 
+
+class mf_cosmo_params(C.Structure):
+    _fields_ = [("Omega_m", C.c_double), ("Omega_b", C.c_double), ("h", C.c_double), ("sigma_8", C.c_double),
+                ("n_s", C.c_double), ("Omega_L", C.c_double), ("Tcmb", C.c_double), ("m_nu1", C.c_double),
+                ("N_ur", C.c_double), ("w_0", C.c_double), ("w_a", C.c_double), ("zero_radiation", C.c_int)]
+
+
+class mf_cosmo_scalars(C.Structure):
+    _fields_ = [("Dplus", C.c_double), ("vfac", C.c_double), ("f", C.c_double), ("pnorm", C.c_double),
+                ("sigma8_measured", C.c_double), ("n_s", C.c_double), ("h", C.c_double), ("H0", C.c_double),
+                ("Omega_m", C.c_double), ("Omega_b", C.c_double), ("Omega_r", C.c_double),
+                ("Omega_DE", C.c_double), ("Tcmb", C.c_double)]
+
+
+class mf_ic_params(C.Structure):
+    _fields_ = [("ngrid", C.c_int), ("boxlen", C.c_double), ("zstart", C.c_double), ("lpt_order", C.c_int),
+                ("lattice", C.c_int), ("precision", C.c_int), ("convolver", C.c_int), ("fixing", C.c_int),
+                ("inversion", C.c_int), ("plt", C.c_int), ("cosmo", mf_cosmo_scalars),
+                ("tk_table", C.c_void_p), ("lunit", C.c_double), ("vunit", C.c_double), ("out_kind", C.c_int),
+                ("pos64", C.c_int), ("id64", C.c_int)]
+
+
+class mf_particles(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("ids", C.c_void_p), ("npart", C.c_int64),
+                ("location", C.c_int)]
+
+
+MF_OUT_PARTICLES, MF_OUT_FIELDS = 0, 1
+MF_LOC_HOST, MF_LOC_DEVICE = 0, 1
+
+SIGNATURES.update({
+    "mf_cosmo_params_default": (None, [C.POINTER(mf_cosmo_params)]),
+    "mf_cosmology_compute": (C.c_int, [C.POINTER(mf_cosmo_params), C.c_double, C.POINTER(mf_cosmo_scalars)]),
+    "mf_eh_transfer": (C.c_int, [C.POINTER(mf_cosmo_params), C.c_void_p, C.c_void_p, C.c_size_t]),
+    "mf_white_noise_host": (C.c_int, [C.c_int, C.c_uint64, C.c_void_p, C.c_int]),
+    "mf_ic_output_size": (C.c_int, [C.POINTER(mf_ic_params), C.POINTER(C.c_int64), C.POINTER(C.c_size_t),
+                                    C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "mf_ic_device_footprint": (C.c_int, [C.POINTER(mf_ic_params), C.POINTER(C.c_size_t)]),
+    "mf_ic_create": (C.c_int, [C.c_void_p, C.POINTER(mf_ic_params), C.POINTER(C.c_void_p)]),
+    "mf_ic_destroy": (C.c_int, [C.c_void_p]),
+    "mf_ic_set_noise": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "mf_ic_run": (C.c_int, [C.c_void_p, C.POINTER(mf_particles)]),
+    "mf_ic_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "mf_ic_get_potential": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_ic_get_noise": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+})
+
 _lib = None
 
 

@@ -1,0 +1,187 @@
+"""IC-level API: host cosmology, the white-noise plugin and the LPT pipeline
+of ic_generator::run (src/ic_generator.cc:90-948) over libmfgpu's C ABI
+(include/monofonic_gb300_ic.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from . import Context, Grid_FFT, lib, _check, MFError
+
+LATTICES = {"sc": 0, "bcc": 1, "fcc": 2, "rsc": 3}
+
+
+@dataclass
+class Cosmology:
+    """[cosmology] section, ParameterSet = none (cosmology_parameters.hh:84-150)."""
+    Omega_m: float = 0.3099
+    Omega_b: float = 0.0488
+    h: float = 0.6774
+    sigma_8: float = 0.8102
+    n_s: float = 0.9667
+    Omega_L: float = -1.0
+    Tcmb: float = -1.0
+    m_nu1: float = -1.0
+    N_ur: float = -1.0
+    w_0: float = -1.0
+    w_a: float = 0.0
+    zero_radiation: bool = False
+
+    def to_c(self):
+        p = L.mf_cosmo_params()
+        for f in ("Omega_m", "Omega_b", "h", "sigma_8", "n_s", "Omega_L", "Tcmb", "m_nu1", "N_ur", "w_0", "w_a"):
+            setattr(p, f, float(getattr(self, f)))
+        p.zero_radiation = int(self.zero_radiation)
+        return p
+
+
+def cosmology_scalars(cosmo: Cosmology, zstart: float):
+    """cosmology::calculator scalars at z_start (D+, vfac, pnorm, ...)."""
+    out = L.mf_cosmo_scalars()
+    rc = lib().mf_cosmology_compute(C.byref(cosmo.to_c()), float(zstart), C.byref(out))
+    if rc != L.MF_OK:
+        raise MFError(rc, "mf_cosmology_compute")
+    return out
+
+
+def eh_transfer(cosmo: Cosmology, k):
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    out = np.empty_like(k)
+    rc = lib().mf_eh_transfer(C.byref(cosmo.to_c()), k.ctypes.data, out.ctypes.data, k.size)
+    if rc != L.MF_OK:
+        raise MFError(rc, "mf_eh_transfer")
+    return out
+
+
+def white_noise(n: int, seed: int, nthreads: int = 0) -> np.ndarray:
+    """Project RNG plugin: n^3 float64 N(0,1) noise (Philox4x32-10 + Box-Muller)."""
+    out = np.empty((n, n, n), dtype=np.float64)
+    rc = lib().mf_white_noise_host(int(n), C.c_uint64(seed), out.ctypes.data, int(nthreads))
+    if rc != L.MF_OK:
+        raise MFError(rc, "mf_white_noise_host")
+    return out
+
+
+@dataclass
+class ICConfig:
+    """[setup] keys of the path (ic_generator.cc:98-149) plus output options."""
+    ngrid: int
+    boxlen: float
+    zstart: float
+    lpt_order: int = 3
+    lattice: str = "sc"
+    precision: str = "f64"
+    convolver: str = "orszag"
+    fixing: bool = False
+    inversion: bool = False
+    plt: bool = False
+    lunit: float = 1.0
+    vunit: float = 1.0
+    out_kind: str = "particles"
+    pos64: bool = True
+    id64: bool = True
+
+    def to_c(self, scalars, tk_table=None):
+        p = L.mf_ic_params()
+        p.ngrid = self.ngrid
+        p.boxlen = self.boxlen
+        p.zstart = self.zstart
+        p.lpt_order = self.lpt_order
+        p.lattice = LATTICES[self.lattice]
+        p.precision = L.MF_PREC_F64 if self.precision == "f64" else L.MF_PREC_F32
+        p.convolver = L.MF_CONV_ORSZAG if self.convolver == "orszag" else L.MF_CONV_NAIVE
+        p.fixing = int(self.fixing)
+        p.inversion = int(self.inversion)
+        p.plt = int(self.plt)
+        p.cosmo = scalars
+        p.tk_table = tk_table.ctypes.data if tk_table is not None else None
+        p.lunit = self.lunit
+        p.vunit = self.vunit
+        p.out_kind = L.MF_OUT_PARTICLES if self.out_kind == "particles" else L.MF_OUT_FIELDS
+        p.pos64 = int(self.pos64)
+        p.id64 = int(self.id64)
+        return p
+
+
+class ICGenerator:
+    """Device-resident LPT pipeline for one parameter set."""
+
+    def __init__(self, ctx: Context, cfg: ICConfig, scalars, tk_table=None):
+        self.ctx, self.cfg = ctx, cfg
+        self._tk = None if tk_table is None else np.ascontiguousarray(tk_table, dtype=np.float64)
+        self.params = cfg.to_c(scalars, self._tk)
+        p = C.c_void_p()
+        _check(ctx.ptr, lib().mf_ic_create(ctx.ptr, C.byref(self.params), C.byref(p)))
+        self.ptr = p
+        np_, pb, vb, ib = C.c_int64(), C.c_size_t(), C.c_size_t(), C.c_size_t()
+        lib().mf_ic_output_size(C.byref(self.params), C.byref(np_), C.byref(pb), C.byref(vb), C.byref(ib))
+        self.npart, self.pos_bytes, self.vel_bytes, self.id_bytes = np_.value, pb.value, vb.value, ib.value
+
+    def set_noise(self, noise: np.ndarray):
+        a = np.ascontiguousarray(noise, dtype=np.float64)
+        _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, a.ctypes.data, L.MF_LOC_HOST))
+
+    def set_noise_device(self, dptr: int):
+        _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, C.c_void_p(dptr), L.MF_LOC_DEVICE))
+
+    def run(self, to_host: bool = True):
+        """Run the pipeline; returns (pos, vel, ids) numpy arrays, or device
+        pointers when to_host is False."""
+        cfg = self.cfg
+        out = L.mf_particles()
+        if to_host:
+            if cfg.out_kind == "fields":
+                pos = np.empty((3, cfg.ngrid, cfg.ngrid, cfg.ngrid))
+                vel = np.empty_like(pos)
+                ids = None
+            else:
+                rt = np.float64 if cfg.pos64 else np.float32
+                pos = np.empty((self.npart, 3), dtype=rt)
+                vel = np.empty((self.npart, 3), dtype=rt)
+                ids = np.empty(self.npart, dtype=np.uint64 if cfg.id64 else np.uint32)
+            out.pos, out.vel = pos.ctypes.data, vel.ctypes.data
+            out.ids = ids.ctypes.data if ids is not None else None
+            out.location = L.MF_LOC_HOST
+            _check(self.ctx.ptr, lib().mf_ic_run(self.ptr, C.byref(out)))
+            return pos, vel, ids
+        out.location = L.MF_LOC_DEVICE
+        _check(self.ctx.ptr, lib().mf_ic_run(self.ptr, C.byref(out)))
+        return out.pos, out.vel, out.ids
+
+    def stage_times(self):
+        ms = (C.c_double * 8)()
+        lib().mf_ic_stage_times(self.ptr, ms)
+        return list(ms)
+
+    def potential(self, which: int) -> np.ndarray:
+        """k-space potential (unscaled) of the last run: 0 phi, 1 phi2, 2 phi3, 3-5 A3."""
+        g = C.c_void_p()
+        _check(self.ctx.ptr, lib().mf_ic_get_potential(self.ptr, int(which), C.byref(g)))
+        n = self.cfg.ngrid
+        dt = np.float64 if self.cfg.precision == "f64" else np.float32
+        a = np.empty((n, n, n + 2), dtype=dt)
+        _check(self.ctx.ptr, lib().mf_grid_download(g, a.ctypes.data))
+        return a.view(np.complex128 if dt == np.float64 else np.complex64).reshape(n, n, n // 2 + 1)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().mf_ic_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def device_footprint(cfg: ICConfig, scalars) -> int:
+    b = C.c_size_t()
+    p = cfg.to_c(scalars)
+    rc = lib().mf_ic_device_footprint(C.byref(p), C.byref(b))
+    if rc != L.MF_OK:
+        raise MFError(rc, "mf_ic_device_footprint")
+    return b.value

@@ -250,6 +250,12 @@ class CosmoScalars:
     params: dict = field(default_factory=dict)
 
 
+def scalars_from(p, Dplus, vfac, pnorm):
+    """CosmoScalars sharing externally computed D+, vfac and pnorm (the
+    scalars cross the boundary from one host calculator to both sides)."""
+    return CosmoScalars(Dplus=Dplus, vfac=vfac, pnorm=pnorm, n_s=p["n_s"], params=p)
+
+
 def cosmo_calculator(p, zstart):
     """cosmology::calculator ctor (cosmology_calculator.hh:166-210) plus
     get_growth_factor/get_vfact (:334-363) and compute_pnorm_from_sigma8 (:439-463)."""
@@ -272,9 +278,12 @@ def cosmo_calculator(p, zstart):
 
     # GSL QAG-61 to rel 1e-10 over [kmin, kmax] = [1e-4, 1e4]
     # (cosmology_calculator.hh:62-83, 439-452); QUADPACK over log-spaced pieces here
+    import warnings
     edges = np.logspace(-4, 4, 161)
-    sig = sum(quad(dsigma8, a, b, epsabs=0, epsrel=1e-13, limit=200)[0]
-              for a, b in zip(edges[:-1], edges[1:]))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        sig = sum(quad(dsigma8, a, b, epsabs=0, epsrel=1e-12, limit=400)[0]
+                  for a, b in zip(edges[:-1], edges[1:]))
     sigma8_meas = math.sqrt(4.0 * math.pi * sig)
     pnorm = p["sigma_8"] ** 2 / sigma8_meas ** 2
     return CosmoScalars(Dplus=Dplus, vfac=vfac, pnorm=pnorm, n_s=ns, params=p)

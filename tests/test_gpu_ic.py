@@ -1,0 +1,138 @@
+"""End-to-end LPT pipeline (ic_generator::run, src/ic_generator.cc:90-948)
+against the oracle on identical white noise and shared cosmology scalars.
+Tolerances: plain FP64 path rel-L2 <= 1e-12; FP32-bulk displacement rel-L2
+<= 1e-5 against the FP64 oracle."""
+import numpy as np
+import pytest
+
+from oracle import lpt_oracle as O
+from tests.ic_helpers import lattice_q, rel_l2, setup
+
+pytestmark = pytest.mark.gpu
+F64_TOL = 1e-12
+F32_TOL = 1e-5
+
+
+def run_gpu(ctx, cfg, sc, noise):
+    from monofonic_gb300 import ic
+    g = ic.ICGenerator(ctx, cfg, sc)
+    g.set_noise(noise)
+    out = g.run()
+    return g, out
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_potentials_f64(ctx, order):
+    """phi, phi2, phi3, A3 (ic_generator.cc:449-546) before growth scaling."""
+    from monofonic_gb300 import ic
+    n, L, z = 32, 100.0, 49.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 12345)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=order)
+    g, _ = run_gpu(ctx, cfg, sc, noise)
+    ref = O.lpt_potentials(noise, L, order, osc)
+    D = sc.Dplus
+    gs = [-D, -3.0 / 7.0 * D * D, D ** 3 / 3.0] + [D ** 3 / 7.0] * 3
+    refs = [ref.phi, ref.phi2, ref.phi3] + (ref.A3 or [])
+    for w in range(len(refs) if order > 2 else order):
+        assert rel_l2(g.potential(w) * gs[w], refs[w]) < F64_TOL, f"potential {w}"
+
+
+def test_config1_2lpt_fields_f64(ctx):
+    """2LPT, N=64, SC, L=100, z=49, FP64 field output (displacements and
+    velocities as float64 grids)."""
+    from monofonic_gb300 import ic
+    n, L, z = 64, 100.0, 49.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 12345)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2, out_kind="fields")
+    _, (dx, vx, _) = run_gpu(ctx, cfg, sc, noise)
+    f = O.lpt_potentials(noise, L, 2, osc)
+    for d in range(3):
+        rd = O.c2r(O.displacement_k(f, L, d, 2), n)
+        rv = O.c2r(O.displacement_k(f, L, d, 2, vel=True, vfac=osc.vfac), n)
+        assert rel_l2(dx[d], rd) < F64_TOL
+        assert rel_l2(vx[d], rv) < F64_TOL
+
+
+@pytest.mark.parametrize("lattice", ["sc", "bcc"])
+@pytest.mark.parametrize("order", [2, 3])
+def test_particles_f64(ctx, lattice, order):
+    from monofonic_gb300 import ic
+    n, L, z = 32, 500.0 * 32 / 256, 24.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 777)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=order, lattice=lattice, lunit=L, vunit=L)
+    _, (pos, vel, ids) = run_gpu(ctx, cfg, sc, noise)
+    f = O.lpt_potentials(noise, L, order, osc)
+    rpos, rvel, rids = O.particles(f, L, order, osc.vfac, lattice=O_LAT[lattice], lunit=L, vunit=L)
+    q = lattice_q(n, O_LAT[lattice], L)
+    assert rel_l2(pos - q, rpos - q) < F64_TOL
+    assert rel_l2(vel, rvel) < F64_TOL
+    assert np.array_equal(ids, rids)
+
+
+O_LAT = {"sc": 0, "bcc": 1, "fcc": 2, "rsc": 3}
+
+
+def test_ids_u32_and_float_positions(ctx):
+    from monofonic_gb300 import ic
+    n, L, z = 16, 50.0, 30.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 3)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2, lattice="bcc", pos64=False, id64=False)
+    _, (pos, vel, ids) = run_gpu(ctx, cfg, sc, noise)
+    assert pos.dtype == np.float32 and ids.dtype == np.uint32
+    assert np.array_equal(ids.astype(np.uint64), O.particle_ids(n, 1))
+    f = O.lpt_potentials(noise, L, 2, osc)
+    rpos, rvel, _ = O.particles(f, L, 2, osc.vfac, lattice=1)
+    # positions stored as float (set_pos32): float rounding of q+Psi
+    assert np.max(np.abs(pos - rpos.astype(np.float32))) <= 2 * np.finfo(np.float32).eps
+
+
+@pytest.mark.parametrize("order", [2, 3])
+def test_f32_bulk_error_per_order(ctx, order):
+    """FP32-bulk form against the FP64 oracle: displacement rel-L2 <= 1e-5."""
+    from monofonic_gb300 import ic
+    n, L, z = 64, 250.0, 24.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 4242)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=order, precision="f32", out_kind="fields")
+    g, (dx, vx, _) = run_gpu(ctx, cfg, sc, noise)
+    f = O.lpt_potentials(noise, L, order, osc)
+    for d in range(3):
+        rd = O.c2r(O.displacement_k(f, L, d, order), n)
+        rv = O.c2r(O.displacement_k(f, L, d, order, vel=True, vfac=osc.vfac), n)
+        assert rel_l2(dx[d], rd) < F32_TOL
+        assert rel_l2(vx[d], rv) < F32_TOL
+    D = sc.Dplus
+    gs = [-D, -3.0 / 7.0 * D * D, D ** 3 / 3.0]
+    refs = [f.phi, f.phi2, f.phi3]
+    for w in range(order):
+        assert rel_l2(g.potential(w) * gs[w], refs[w]) < F32_TOL
+
+
+def test_naive_fixing_inversion(ctx):
+    from monofonic_gb300 import ic
+    n, L, z = 32, 100.0, 40.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 99)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=3, convolver="naive", fixing=True, inversion=True,
+                      out_kind="fields")
+    _, (dx, vx, _) = run_gpu(ctx, cfg, sc, noise)
+    f = O.lpt_potentials(noise, L, 3, osc, convolver="naive", fixing=True, inversion=True)
+    for d in range(3):
+        assert rel_l2(dx[d], O.c2r(O.displacement_k(f, L, d, 3), n)) < F64_TOL
+
+
+def test_rejects_bad_params(ctx):
+    from monofonic_gb300 import ic, MFError
+    cosmo, sc, osc = setup(20.0)
+    with pytest.raises(MFError):
+        ic.ICGenerator(ctx, ic.ICConfig(ngrid=100, boxlen=1.0, zstart=20.0), sc)
+    with pytest.raises(MFError):
+        ic.ICGenerator(ctx, ic.ICConfig(ngrid=32, boxlen=1.0, zstart=20.0, lpt_order=4), sc)
+    g = ic.ICGenerator(ctx, ic.ICConfig(ngrid=16, boxlen=10.0, zstart=20.0, lpt_order=1), sc)
+    with pytest.raises(MFError) as e:
+        g.run()
+    assert "MF_ERR_STATE" in str(e.value)
