@@ -1,0 +1,402 @@
+#!/usr/bin/env python3
+"""Benchmark: 3LPT particles/s at 512^3 on one GB300, FP32-bulk vs FP64 plain.
+
+Workload (one "step" = one full initial-condition pass over one synthetic
+realization): 3LPT, Orszag 3/2 dealiasing (padded 768^3 convolutions), BCC
+lattice of 2 x 512^3 particles, box 1000 Mpc/h, z_start = 24, Eisenstein & Hu
+transfer function, seeded N(0,1) white noise (synthetic; no dataset).
+
+  value   particles/s of the FP32-bulk form, white noise already resident in
+          HBM when the timed region starts, particles (positions, velocities,
+          IDs) resident in HBM when it ends; CUDA events on the pipeline's
+          stream; the working set (>16 GB) is far larger than L2.
+  e2e     the same through the public C ABI (mf_ic_set_noise + mf_ic_run)
+          with the noise copied from page-locked host memory and all
+          particles copied back to page-locked host memory every step.
+  fp64    the plain FP64 form on the same workload (positions in double).
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement in numpy/scipy, all host threads) on a bounded sample of
+the same workload and extrapolates to one IC.
+
+Multi-GPU: every rank runs an independent realization (replicas; no
+collectives on the data path); value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3LPT particles/s at 512^3: FP32-bulk vs FP64 plain (1 GB300); p50/p99 IC latency"
+UNIT = "particles/s"
+
+WORKLOAD = dict(ngrid=512, boxlen=1000.0, zstart=24.0, lpt_order=3, lattice="bcc")
+COSMO = dict(Omega_m=0.3099, Omega_b=0.0488, h=0.6774, sigma_8=0.8102, n_s=0.9667)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mf", choices=["mf", "reference"])
+    ap.add_argument("--ngrid", type=int, default=512)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per launch of each kernel kind for one 3LPT IC
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(kind: str, n: int, prec_bytes: int) -> float:
+    cs = 2 * prec_bytes
+    M, Kz = 3 * n // 2, n // 2 + 1
+    S_NK, S_MNK, S_MMK = n * n * Kz * cs, M * n * Kz * cs, M * M * Kz * cs
+    if kind == "conv_xinv":
+        return 2 * (S_NK + S_MNK)
+    if kind == "conv_yinv":
+        return 2 * (S_MNK + S_MMK)
+    if kind == "conv_z":
+        return 2 * S_MMK + S_MMK
+    if kind == "conv_yfwd":
+        return S_MMK + S_MNK
+    if kind == "conv_xfwd":
+        # 33 per 3LPT IC: 10 assign (write only), 23 read-modify-write
+        return S_MNK + (10 * S_NK + 23 * 2 * S_NK) / 33.0
+    if kind == "fft_z":
+        return 2 * n * n * (n + 2) * prec_bytes
+    if kind == "fft_col":
+        return 2 * S_NK
+    return float("nan")
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement, bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(n: int, threads: int):
+    """One Orszag convolve2 at N (3 padded transforms + pad/unpad sweeps) and
+    one N-grid r2c+c2r pair, timed; one 3LPT BCC IC is 33 convolve2 plus
+    about 10 N-grid transform pairs (noise, assembly, sub-lattice shifts)."""
+    import numpy as np
+    from oracle import lpt_oracle as O
+    O.set_fft_workers(threads)
+    L = WORKLOAD["boxlen"]
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((n, n, n))
+    t0 = time.perf_counter()
+    X = O.r2c(x)
+    y = O.c2r(X, n)
+    t_pair = time.perf_counter() - t0
+    del y
+    t0 = time.perf_counter()
+    r = O.orszag_conv2(O.hessian(X, L, 0, 1), O.hessian(X, L, 2, 2))
+    t_conv = time.perf_counter() - t0
+    del r, X, x
+    t_ic = 33 * t_conv + 10 * t_pair
+    npart = 2 * n ** 3
+    return {"value": npart / t_ic, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"oracle (numpy/scipy pocketfft, {threads} threads): one Orszag convolve2 at N={n} "
+                       f"({t_conv:.2f} s) + one N={n} r2c/c2r pair ({t_pair:.2f} s), "
+                       f"extrapolated as 33 convolve2 + 10 pairs per 3LPT BCC IC = {t_ic:.1f} s"),
+            "seconds_per_ic": t_ic}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = args.ngrid
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(n, threads)
+        if i >= args.warmup:
+            vals.append(r)
+    v = statistics.median([r["value"] for r in vals])
+    ms = statistics.median([r["seconds_per_ic"] for r in vals]) * 1e3
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"3LPT BCC 2x{n}^3, Orszag M={3 * n // 2}, L=1000, z=24", "impl": "oracle port"},
+            "impl": "reference",
+            "cpu_baseline": {k: vals[-1][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": UNIT},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_mf(args):
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    import monofonic_gb300 as mf
+    from monofonic_gb300 import ic
+
+    n = args.ngrid
+    ctx = mf.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    cosmo = ic.Cosmology(**COSMO)
+    sc = ic.cosmology_scalars(cosmo, WORKLOAD["zstart"])
+    seed = 12345 + 1000 * rank
+    noise_h = ic.white_noise(n, seed)
+    noise_d = torch.from_numpy(noise_h).to(torch.device("cuda", local))
+    torch.cuda.synchronize()
+
+    def make(prec):
+        cfg = ic.ICConfig(ngrid=n, boxlen=WORKLOAD["boxlen"], zstart=WORKLOAD["zstart"],
+                          lpt_order=WORKLOAD["lpt_order"], lattice=WORKLOAD["lattice"], precision=prec,
+                          lunit=WORKLOAD["boxlen"], vunit=WORKLOAD["boxlen"], pos64=(prec == "f64"), id64=True)
+        return ic.ICGenerator(ctx, cfg, sc)
+
+    def timed(gen, steps, warmup, clocks=None, profile=False):
+        for _ in range(warmup):
+            gen.set_noise_device(noise_d.data_ptr())
+            gen.run(to_host=False)
+        barrier()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        c0 = ctx.launch_counts()
+        if profile:
+            ctx.profile(True)
+        if clocks:
+            clocks.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        per = []
+        e0.record(stream)
+        for _ in range(steps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gen.set_noise_device(noise_d.data_ptr())
+            gen.run(to_host=False)
+            b.record(stream)
+            per.append((a, b))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        clk = clocks.stop() if clocks else None
+        prof = ctx.profile_read() if profile else None
+        if profile:
+            ctx.profile(False)
+        c1 = ctx.launch_counts()
+        total_ms = e0.elapsed_time(e1)
+        lat = sorted(a.elapsed_time(b) for a, b in per)
+        barrier()
+        launches = sum(c1[k] - c0[k] for k in c1)
+        return total_ms, lat, prof, clk, launches, stage(gen)
+
+    def stage(gen):
+        names = ["noise_r2c+phi1", "phi2", "phi3", "A3", "positions", "velocities", "ids", "handoff"]
+        return dict(zip(names, [round(x, 3) for x in gen.stage_times()]))
+
+    # ---- FP32-bulk, inputs resident ------------------------------------------
+    gen32 = make("f32")
+    npart = gen32.npart
+    clocks = Clocks(local)
+    total_ms, lat, prof, clk, launches, stages32 = timed(gen32, args.steps, args.warmup, clocks, profile=True)
+    total_ms = max_over_ranks(total_ms)
+    ms_per_step = total_ms / args.steps
+    value = world * npart * args.steps / (total_ms / 1e3)
+
+    # roofline of the dominant kernel kind
+    dom = max((k for k in prof if k != "pointwise"), key=lambda k: prof[k][0])
+    dom_ms, dom_cnt = prof[dom]
+    avg_ms = dom_ms / max(dom_cnt, 1)
+    bpl = algorithmic_bytes(dom, n, 4)
+    achieved = bpl / (avg_ms / 1e3) / 1e9
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    kinds = {k: {"ms_total": round(v[0], 3), "launches": v[1],
+                 "share": round(v[0] / max(sum(x[0] for x in prof.values()), 1e-9), 4),
+                 "GB_s": (round(algorithmic_bytes(k, n, 4) / (v[0] / max(v[1], 1) / 1e3) / 1e9, 1)
+                          if v[1] and k != "pointwise" else None)}
+             for k, v in prof.items()}
+
+    # ---- e2e through the C ABI with page-locked host buffers ------------------
+    e2e = None
+    if not args.no_e2e:
+        pin_noise = ic.PinnedBuffer(noise_h.nbytes)
+        pin_noise.array(np.float64, noise_h.shape)[...] = noise_h
+        pos = ic.PinnedBuffer(gen32.pos_bytes)
+        vel = ic.PinnedBuffer(gen32.vel_bytes)
+        ids = ic.PinnedBuffer(gen32.id_bytes)
+        for _ in range(max(1, args.warmup)):
+            gen32.set_noise_host_ptr(pin_noise.ptr)
+            gen32.run_into(pos.ptr, vel.ptr, ids.ptr)
+        barrier()
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            gen32.set_noise_host_ptr(pin_noise.ptr)
+            gen32.run_into(pos.ptr, vel.ptr, ids.ptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        t = max_over_ranks(e0.elapsed_time(e1))
+        ids_h = ids.array(np.uint64, (npart,))
+        assert ids_h[1] == 2 and ids_h[n ** 3] == 1, "particle IDs wrong after e2e run"
+        e2e = {"value": world * npart * args.steps / (t / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": int(noise_h.nbytes),
+               "d2h_bytes_per_step": int(gen32.pos_bytes + gen32.vel_bytes + gen32.id_bytes),
+               "ms_per_step": t / args.steps}
+        for b in (pin_noise, pos, vel, ids):
+            b.close()
+    gen32.close()
+
+    # ---- FP64 plain ---------------------------------------------------------------
+    fp64 = None
+    if not args.no_fp64:
+        gen64 = make("f64")
+        t64, lat64, prof64, _, _, stages64 = timed(gen64, args.fp64_steps, 1, None, profile=True)
+        t64 = max_over_ranks(t64)
+        ms64 = t64 / args.fp64_steps
+        fp64 = {"value": world * npart / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
+                "speedup_fp32_bulk_vs_fp64": ms64 / ms_per_step,
+                "kernels": {k: {"ms_total": round(v[0], 2), "launches": v[1]} for k, v in prof64.items()},
+                "stages_ms": stages64}
+        gen64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and world == 1:
+        try:
+            cpu = cpu_sample(n, os.cpu_count() or 1)
+            cpu.pop("seconds_per_ic", None)
+        except Exception as ex:  # the baseline must not break the GPU line
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        p50 = lat[len(lat) // 2]
+        p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": (f"3LPT BCC 2x{n}^3 particles, Orszag 3/2 (M={3 * n // 2}), L=1000 Mpc/h, z=24, "
+                                    "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with FP64 order sum and q+Psi"),
+                       "plt": False, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"},
+            "latency_ms": {"p50": p50, "p99": p99},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": "measured" if peaks else "fallback"},
+            "kernels": kinds,
+            "stages_ms": stages32,
+            "e2e": e2e,
+            "fp64_plain": fp64,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_mf(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

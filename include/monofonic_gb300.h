@@ -64,6 +64,21 @@ const char* mf_last_error(const mf_ctx* ctx);
 int mf_ctx_synchronize(mf_ctx* ctx);
 /* library version string */
 const char* mf_version(void);
+/* the context's CUDA stream (cudaStream_t), for event timing by callers */
+int mf_ctx_stream(mf_ctx* ctx, void** stream);
+/* kernel launches issued on the context so far, per kernel kind:
+ * [conv x-inv, conv y-inv, conv z, conv y-fwd, conv x-fwd, fft z, fft col,
+ *  pointwise]; the reference has no counterpart (measurement hook) */
+int mf_ctx_launch_counts(const mf_ctx* ctx, int64_t* counts, int n);
+/* record an event pair around every launch (per-kind device time); the
+ * reference's per-stage get_wtime brackets (src/ic_generator.cc:459-546)
+ * are the host-side analogue */
+int mf_ctx_profile(mf_ctx* ctx, int enable);
+/* sum of profiled device milliseconds and launch counts per kind; clears */
+int mf_ctx_profile_read(mf_ctx* ctx, double* ms, int64_t* counts, int n);
+/* page-locked host memory for streaming transfers (no reference counterpart) */
+int mf_host_alloc(size_t bytes, void** out);
+int mf_host_free(void* p);
 /* 1 if grid size n is supported by the compiled kernels */
 int mf_grid_size_supported(int n);
 

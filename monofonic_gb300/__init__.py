@@ -45,13 +45,38 @@ class Context:
             raise MFError(rc, f"mf_ctx_create(device={device}) failed")
         self.ptr = p
 
+    KERNEL_KINDS = ("conv_xinv", "conv_yinv", "conv_z", "conv_yfwd", "conv_xfwd", "fft_z", "fft_col", "pointwise")
+
     def synchronize(self):
         _check(self.ptr, lib().mf_ctx_synchronize(self.ptr))
 
+    def stream(self) -> int:
+        """cudaStream_t of the context (an integer handle)."""
+        s = C.c_void_p()
+        _check(self.ptr, lib().mf_ctx_stream(self.ptr, C.byref(s)))
+        return s.value or 0
+
+    def launch_counts(self) -> dict:
+        a = np.zeros(8, dtype=np.int64)
+        _check(self.ptr, lib().mf_ctx_launch_counts(self.ptr, a.ctypes.data, 8))
+        return dict(zip(self.KERNEL_KINDS, a.tolist()))
+
+    def profile(self, enable: bool):
+        _check(self.ptr, lib().mf_ctx_profile(self.ptr, int(enable)))
+
+    def profile_read(self) -> dict:
+        """{kind: (device ms summed over launches, launches)} since the last read."""
+        ms = np.zeros(8)
+        cnt = np.zeros(8, dtype=np.int64)
+        _check(self.ptr, lib().mf_ctx_profile_read(self.ptr, ms.ctypes.data, cnt.ctypes.data, 8))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
     def close(self):
+        """Destroy the context; refused (kept alive) while grids,
+        convolvers or pipelines created on it still exist."""
         if getattr(self, "ptr", None):
-            lib().mf_ctx_destroy(self.ptr)
-            self.ptr = None
+            if lib().mf_ctx_destroy(self.ptr) == L.MF_OK:
+                self.ptr = None
 
     def __del__(self):
         try:

@@ -30,6 +30,12 @@ class mf_operand(C.Structure):
 # name -> (restype, argtypes); every C-ABI symbol the header declares
 SIGNATURES = {
     "mf_version": (C.c_char_p, []),
+    "mf_ctx_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "mf_ctx_launch_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "mf_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "mf_ctx_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "mf_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "mf_host_free": (C.c_int, [C.c_void_p]),
     "mf_grid_size_supported": (C.c_int, [C.c_int]),
     "mf_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "mf_ctx_destroy": (C.c_int, [C.c_void_p]),

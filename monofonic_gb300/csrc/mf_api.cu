@@ -22,6 +22,26 @@ int cuda_err(mf_ctx* c, cudaError_t e, const char* where) {
   return set_err(c, code, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+LaunchScope::LaunchScope(mf_ctx* c, int kind) : c_(c), kind_(kind) {
+  ++c_->launches[kind];
+  if (c_->profile) {
+    cudaEvent_t e0 = nullptr;
+    if (c_->event_pool.size() >= 2) {
+      e0 = c_->event_pool.back(); c_->event_pool.pop_back();
+      e1_ = c_->event_pool.back(); c_->event_pool.pop_back();
+    } else {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1_);
+    }
+    cudaEventRecord(e0, c_->stream);
+    c_->prof_events.push_back({kind_, {e0, e1_}});
+  }
+}
+
+LaunchScope::~LaunchScope() {
+  if (e1_) cudaEventRecord(e1_, c_->stream);
+}
+
 bool length_supported(int L) {
   switch (L) {
     case 8: case 12: case 16: case 24: case 32: case 48: case 64: case 72: case 96: case 128: case 144:
@@ -120,11 +140,19 @@ cudaError_t fft3d_r2c(mf_ctx* c, T* data, int n) {
   const cplx<T>* twN = c->tw.get<T>(n, s);
   if (!twH || !twN) return cudaErrorMemoryAllocation;
   const T norm = T(1.0 / std::sqrt((double)n * (double)n * (double)n));
-  cudaError_t e = Launch<T>::z_r2c_plain(H, PlainZOp<T>{data, n, T(1)}, n * n, Kz, twH, twN, s);
+  cudaError_t e;
+  {
+    LaunchScope ls(c, KK_FFT_Z);
+    e = Launch<T>::z_r2c_plain(H, PlainZOp<T>{data, n, T(1)}, n * n, Kz, twH, twN, s);
+  }
   if (e != cudaSuccess) return e;
   cplx<T>* z = reinterpret_cast<cplx<T>*>(data);
-  e = Launch<T>::colfft_plain(n, false, PlainStridedOp<T>{z, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s);
+  {
+    LaunchScope ls(c, KK_FFT_COL);
+    e = Launch<T>::colfft_plain(n, false, PlainStridedOp<T>{z, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s);
+  }
   if (e != cudaSuccess) return e;
+  LaunchScope ls(c, KK_FFT_COL);
   return Launch<T>::colfft_plain(n, false, PlainStridedOp<T>{z, (long long)n * Kz, Kz, norm}, n, Kz, twN, s);
 }
 
@@ -137,10 +165,18 @@ cudaError_t fft3d_c2r(mf_ctx* c, T* data, int n) {
   if (!twH || !twN) return cudaErrorMemoryAllocation;
   const T norm = T(1.0 / std::sqrt((double)n * (double)n * (double)n));
   cplx<T>* z = reinterpret_cast<cplx<T>*>(data);
-  cudaError_t e = Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{z, (long long)n * Kz, Kz, T(1)}, n, Kz, twN, s);
+  cudaError_t e;
+  {
+    LaunchScope ls(c, KK_FFT_COL);
+    e = Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{z, (long long)n * Kz, Kz, T(1)}, n, Kz, twN, s);
+  }
   if (e != cudaSuccess) return e;
-  e = Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{z, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s);
+  {
+    LaunchScope ls(c, KK_FFT_COL);
+    e = Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{z, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s);
+  }
   if (e != cudaSuccess) return e;
+  LaunchScope ls(c, KK_FFT_Z);
   return Launch<T>::z_c2r_plain(H, PlainZOp<T>{data, n, norm}, n * n, Kz, twH, twN, s);
 }
 
@@ -177,13 +213,20 @@ cudaError_t conv_run(mf_conv* cv, const Operand<T>* ops, int nop, cplx<T>* targe
   xo.g = g;
   xo.kfac = kfac;
   xo.scale = scale_in;
-  cudaError_t e = Launch<T>::conv_xinv(M, xo, N, Kz, nop, twM, s);
+  cudaError_t e;
+  {
+    LaunchScope ls(c, KK_CONV_XINV);
+    e = Launch<T>::conv_xinv(M, xo, N, Kz, nop, twM, s);
+  }
   if (e != cudaSuccess) return e;
 
   ConvYInvOp<T> yo{};
   for (int k = 0; k < nop; ++k) { yo.src[k] = B[k]; yo.dst[k] = B[k]; }
   yo.g = g;
-  e = Launch<T>::conv_yinv(M, yo, M, Kz, nop, twM, s);
+  {
+    LaunchScope ls(c, KK_CONV_YINV);
+    e = Launch<T>::conv_yinv(M, yo, M, Kz, nop, twM, s);
+  }
   if (e != cudaSuccess) return e;
 
   ZConvArgs<T> za{};
@@ -196,11 +239,17 @@ cudaError_t conv_run(mf_conv* cv, const Operand<T>* ops, int nop, cplx<T>* targe
   za.out_stride = Kz;
   za.nlines = M * M;
   za.out_scale = T(1);
-  e = Launch<T>::z_conv(H, za, twH, twM, s);
+  {
+    LaunchScope ls(c, KK_CONV_Z);
+    e = Launch<T>::z_conv(H, za, twH, twM, s);
+  }
   if (e != cudaSuccess) return e;
 
   ConvYFwdOp<T> yf{B[nop - 1], B[nop - 1], g};
-  e = Launch<T>::conv_yfwd(M, yf, M, Kz, twM, s);
+  {
+    LaunchScope ls(c, KK_CONV_YFWD);
+    e = Launch<T>::conv_yfwd(M, yf, M, Kz, twM, s);
+  }
   if (e != cudaSuccess) return e;
 
   ConvXFwdOp<T> xf{};
@@ -212,6 +261,7 @@ cudaError_t conv_run(mf_conv* cv, const Operand<T>* ops, int nop, cplx<T>* targe
   xf.x = x;
   xf.post_invlap = post_invlap;
   xf.kfac = kfac;
+  LaunchScope ls(c, KK_CONV_XFWD);
   return Launch<T>::conv_xfwd(M, xf, N, Kz, twM, s);
 }
 
@@ -249,9 +299,13 @@ extern "C" int mf_ctx_create(int device, mf_ctx** out) {
 
 extern "C" int mf_ctx_destroy(mf_ctx* c) {
   if (!c) return MF_ERR_ARG;
+  if (c->children > 0)
+    return set_err(c, MF_ERR_STATE, "mf_ctx_destroy: " + std::to_string(c->children) + " objects still alive on this context");
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   c->tw.release();
+  for (auto& rec : c->prof_events) { cudaEventDestroy(rec.second.first); cudaEventDestroy(rec.second.second); }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
   return MF_OK;
@@ -288,6 +342,7 @@ extern "C" int mf_grid_create(mf_ctx* c, int n, double boxlen, int prec, int spa
     delete g;
     return cuda_err(c, e, "mf_grid_create: cudaMalloc");
   }
+  ++c->children;
   *out = g;
   return MF_OK;
 }
@@ -297,6 +352,7 @@ extern "C" int mf_grid_destroy(mf_grid* g) {
   cudaSetDevice(g->ctx->device);
   cudaStreamSynchronize(g->ctx->stream);
   cudaFree(g->d);
+  --g->ctx->children;
   delete g;
   return MF_OK;
 }
@@ -390,6 +446,7 @@ extern "C" int mf_grid_scale(mf_grid* g, double x) {
   if (!g) return MF_ERR_ARG;
   cudaSetDevice(g->ctx->device);
   const size_t nr = grid_reals(g->n);
+  LaunchScope ls(g->ctx, KK_POINTWISE);
   cudaError_t e = (g->prec == MF_PREC_F64) ? pw_scale<double>((double*)g->d, nr, x, g->ctx->stream)
                                            : pw_scale<float>((float*)g->d, nr, (float)x, g->ctx->stream);
   return cuda_err(g->ctx, e, "mf_grid_scale");
@@ -399,6 +456,7 @@ extern "C" int mf_grid_zero_dc(mf_grid* g) {
   if (!g) return MF_ERR_ARG;
   if (g->space != MF_SPACE_K) return set_err(g->ctx, MF_ERR_STATE, "mf_grid_zero_dc: real-space branch not supported on the device");
   cudaSetDevice(g->ctx->device);
+  LaunchScope ls(g->ctx, KK_POINTWISE);
   cudaError_t e = (g->prec == MF_PREC_F64) ? pw_zero_dc<double>((double*)g->d, g->ctx->stream)
                                            : pw_zero_dc<float>((float*)g->d, g->ctx->stream);
   return cuda_err(g->ctx, e, "mf_grid_zero_dc");
@@ -409,6 +467,7 @@ extern "C" int mf_grid_inverse_laplacian(mf_grid* g) {
   int rc = mf_grid_fft_forward(g, 1);
   if (rc) return rc;
   const double kfac = 2.0 * M_PI / g->L;
+  LaunchScope ls(g->ctx, KK_POINTWISE);
   cudaError_t e = (g->prec == MF_PREC_F64)
                       ? pw_invlap<double>((cplx<double>*)g->d, g->n, kfac, g->ctx->stream)
                       : pw_invlap<float>((cplx<float>*)g->d, g->n, kfac, g->ctx->stream);
@@ -503,6 +562,7 @@ extern "C" int mf_conv_create(mf_ctx* c, int n, double boxlen, int prec, int kin
       return rc;
     }
   }
+  ++c->children;
   *out = cv;
   return MF_OK;
 }
@@ -513,6 +573,7 @@ extern "C" int mf_conv_destroy(mf_conv* cv) {
   cudaStreamSynchronize(cv->ctx->stream);
   if (cv->fbuf) mf_grid_destroy(cv->fbuf);
   cudaFree(cv->work);
+  --cv->ctx->children;
   delete cv;
   return MF_OK;
 }
@@ -605,4 +666,56 @@ extern "C" int mf_conv_convolve3(mf_conv* cv, const mf_operand* a, const mf_oper
                                  mf_grid* out, int op, double x) {
   const mf_operand* ops[3] = {a, b, c3};
   return conv_entry(cv, ops, 3, out, op, x, 0);
+}
+
+// ---------------------------------------------------------------------------
+// measurement hooks
+// ---------------------------------------------------------------------------
+extern "C" int mf_ctx_stream(mf_ctx* c, void** stream) {
+  if (!c || !stream) return MF_ERR_ARG;
+  *stream = (void*)c->stream;
+  return MF_OK;
+}
+
+extern "C" int mf_ctx_launch_counts(const mf_ctx* c, int64_t* counts, int n) {
+  if (!c || !counts) return MF_ERR_ARG;
+  for (int k = 0; k < n && k < KK_COUNT; ++k) counts[k] = c->launches[k];
+  return MF_OK;
+}
+
+extern "C" int mf_ctx_profile(mf_ctx* c, int enable) {
+  if (!c) return MF_ERR_ARG;
+  c->profile = enable != 0;
+  return MF_OK;
+}
+
+extern "C" int mf_ctx_profile_read(mf_ctx* c, double* ms, int64_t* counts, int n) {
+  if (!c || !ms || !counts) return MF_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "mf_ctx_profile_read");
+  for (int k = 0; k < n; ++k) { ms[k] = 0; counts[k] = 0; }
+  for (auto& rec : c->prof_events) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, rec.second.first, rec.second.second) == cudaSuccess && rec.first < n) {
+      ms[rec.first] += t;
+      counts[rec.first] += 1;
+    }
+    c->event_pool.push_back(rec.second.first);
+    c->event_pool.push_back(rec.second.second);
+  }
+  c->prof_events.clear();
+  return MF_OK;
+}
+
+extern "C" int mf_host_alloc(size_t bytes, void** out) {
+  if (!out) return MF_ERR_ARG;
+  *out = nullptr;
+  if (cudaHostAlloc(out, bytes, cudaHostAllocPortable) != cudaSuccess) return MF_ERR_OOM;
+  return MF_OK;
+}
+
+extern "C" int mf_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+  return MF_OK;
 }

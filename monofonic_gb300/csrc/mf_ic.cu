@@ -255,11 +255,13 @@ int run_impl(mf_ic* ic, mf_particles* out) {
       CK(cudaMemcpyAsync(ic->amp + ic->nk2, p.tk_table, sizeof(double) * ic->nk2, cudaMemcpyHostToDevice, s));
       tk = ic->amp + ic->nk2;
     }
+    LaunchScope ls0(c, KK_POINTWISE);
     k_amp_table<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ic->amp, ic->nk2, kfac, 0.5 * p.cosmo.n_s,
                                                        std::sqrt(p.cosmo.pnorm), eh, tk);
     CK(cudaGetLastError());
     const double volfac = std::pow(L / n / 2.0 / M_PI, 1.5);
     const double sgn = (p.inversion ? -1.0 : 1.0) / volfac;
+    LaunchScope ls1(c, KK_POINTWISE);
     k_phi1<T><<<blocks_for(nk), kThreads, 0, s>>>((cplx<T>*)ic->wn->d, (cplx<T>*)ic->f[0]->d, n, kfac, ic->amp, sgn,
                                                    p.fixing);
     CK(cudaGetLastError());
@@ -372,11 +374,15 @@ int run_impl(mf_ic* ic, mf_particles* out) {
       for (int ish = 0; ish < overload; ++ish) {
         a.shift = ish > 0;
         for (int q = 0; q < 3; ++q) a.s[q] = kShifts[p.lattice][ish][q];
-        k_assemble<T><<<blocks_for(nk), kThreads, 0, s>>>(a, (cplx<T>*)tmpr, n, kfac);
+        {
+          LaunchScope ls(c, KK_POINTWISE);
+          k_assemble<T><<<blocks_for(nk), kThreads, 0, s>>>(a, (cplx<T>*)tmpr, n, kfac);
+        }
         CK(cudaGetLastError());
         CK(fft3d_c2r<T>(c, tmpr, n));
         const size_t n3 = (size_t)n * n * n;
         const double sd = kShifts[p.lattice][ish][d];
+        LaunchScope ls(c, KK_POINTWISE);
         if (fields) {
           k_lattice<T, double><<<blocks_for(n3), kThreads, 0, s>>>(tmpr, n, (double*)dst, d, 0, 0.0, 0.0, 0, 1);
         } else if (p.pos64) {
@@ -393,6 +399,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
   }
   // ---- particle IDs (particle_generator.hh:212-253) ------------------------
   if (!fields) {
+    LaunchScope ls(c, KK_POINTWISE);
     if (p.id64)
       k_ids<uint64_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint64_t*)ic->dids, n, overload, 0);
     else
@@ -471,6 +478,7 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->dids);
   for (auto& e : ic->ev)
     if (e) cudaEventDestroy(e);
+  --c->children;
   delete ic;
   return MF_OK;
 }
@@ -484,6 +492,7 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   mf_ic* ic = new (std::nothrow) mf_ic();
   if (!ic) return MF_ERR_OOM;
   ic->ctx = c;
+  ++c->children;
   ic->p = *p;
   ic->p.tk_table = nullptr;
   const int n = p->ngrid;

@@ -3,16 +3,54 @@
 
 #include <cuda_runtime.h>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/monofonic_gb300.h"
 #include "mf_internal.h"
+
+namespace mf {
+// kernel kinds for launch counting and in-stream event profiling
+enum KernelKind : int {
+  KK_CONV_XINV = 0,
+  KK_CONV_YINV = 1,
+  KK_CONV_Z = 2,
+  KK_CONV_YFWD = 3,
+  KK_CONV_XFWD = 4,
+  KK_FFT_Z = 5,
+  KK_FFT_COL = 6,
+  KK_POINTWISE = 7,
+  KK_COUNT = 8
+};
+}  // namespace mf
 
 struct mf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   mf::TwiddleCache tw;
   std::string err;
+  int children = 0;  // live grids, convolvers and pipelines on this context
+  // launch accounting
+  long long launches[mf::KK_COUNT] = {};
+  bool profile = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_events;
+  std::vector<cudaEvent_t> event_pool;
 };
+
+namespace mf {
+// RAII bracket of one kernel launch: counts it and, when profiling is on,
+// records an event pair around it on the context's stream
+class LaunchScope {
+ public:
+  LaunchScope(mf_ctx* c, int kind);
+  ~LaunchScope();
+
+ private:
+  mf_ctx* c_;
+  int kind_;
+  cudaEvent_t e1_ = nullptr;
+};
+}  // namespace mf
 
 struct mf_grid {
   mf_ctx* ctx = nullptr;

@@ -127,6 +127,17 @@ class ICGenerator:
     def set_noise_device(self, dptr: int):
         _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, C.c_void_p(dptr), L.MF_LOC_DEVICE))
 
+    def set_noise_host_ptr(self, hptr: int):
+        """noise from a host pointer (e.g. page-locked memory of mf_host_alloc)."""
+        _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, C.c_void_p(hptr), L.MF_LOC_HOST))
+
+    def run_into(self, pos_ptr: int, vel_ptr: int, ids_ptr: int):
+        """run and copy the particles into caller-owned host buffers."""
+        out = L.mf_particles()
+        out.pos, out.vel, out.ids = pos_ptr, vel_ptr, ids_ptr
+        out.location = L.MF_LOC_HOST
+        _check(self.ctx.ptr, lib().mf_ic_run(self.ptr, C.byref(out)))
+
     def run(self, to_host: bool = True):
         """Run the pipeline; returns (pos, vel, ids) numpy arrays, or device
         pointers when to_host is False."""
@@ -169,6 +180,32 @@ class ICGenerator:
     def close(self):
         if getattr(self, "ptr", None):
             lib().mf_ic_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host buffer (mf_host_alloc)."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        rc = lib().mf_host_alloc(C.c_size_t(int(nbytes)), C.byref(p))
+        if rc != L.MF_OK:
+            raise MFError(rc, f"mf_host_alloc({nbytes})")
+        self.ptr, self.nbytes = p.value, int(nbytes)
+
+    def array(self, dtype, shape):
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().mf_host_free(C.c_void_p(self.ptr))
             self.ptr = None
 
     def __del__(self):

@@ -341,11 +341,35 @@ def white_noise(n, seed):
 # ----------------------------------------------------------------------------
 # Grid_FFT essentials (include/grid_fft.hh, src/grid_fft.cc)
 # ----------------------------------------------------------------------------
+_FFT_WORKERS = 1
+
+
+def set_fft_workers(n: int):
+    """Threads for the oracle's transforms (the reference's FFTW threads,
+    src/main.cc:156-174); >1 switches to scipy's multithreaded pocketfft."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = max(1, int(n))
+
+
+def _rfftn(x):
+    if _FFT_WORKERS > 1:
+        import scipy.fft as sf
+        return sf.rfftn(x, axes=(0, 1, 2), workers=_FFT_WORKERS)
+    return np.fft.rfftn(x, axes=(0, 1, 2))
+
+
+def _irfftn(X, n):
+    if _FFT_WORKERS > 1:
+        import scipy.fft as sf
+        return sf.irfftn(X, s=(n, n, n), axes=(0, 1, 2), workers=_FFT_WORKERS)
+    return np.fft.irfftn(X, s=(n, n, n), axes=(0, 1, 2))
+
+
 def r2c(x):
     """FourierTransformForward + ApplyNorm (grid_fft.cc:199-235): FFTW r2c
     (sign -1) of an n^3 real array, scaled by 1/sqrt(n^3)."""
     n = x.shape[0]
-    return np.fft.rfftn(x, axes=(0, 1, 2)) / math.sqrt(float(n) ** 3)
+    return _rfftn(x) / math.sqrt(float(n) ** 3)
 
 
 def c2r(X, n=None):
@@ -357,7 +381,7 @@ def c2r(X, n=None):
     and numpy's irfftn."""
     if n is None:
         n = X.shape[0]
-    return np.fft.irfftn(X, s=(n, n, n), axes=(0, 1, 2)) * (float(n) ** 3 / math.sqrt(float(n) ** 3))
+    return _irfftn(X, n) * (float(n) ** 3 / math.sqrt(float(n) ** 3))
 
 
 def kvec_1d(n, L):

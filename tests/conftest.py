@@ -17,4 +17,5 @@ def ctx():
     import monofonic_gb300 as mf
     c = mf.Context(0)
     yield c
-    c.close()
+    # objects created by tests hold references to the context; it is
+    # destroyed when the last of them is collected

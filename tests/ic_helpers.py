@@ -17,7 +17,9 @@ def setup(zstart):
 
 
 def rel_l2(a, b):
-    return float(np.linalg.norm(np.asarray(a, dtype=np.float64) - b) / np.linalg.norm(b))
+    a = np.asarray(a)
+    a = a.astype(np.complex128) if np.iscomplexobj(a) else a.astype(np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
 def lattice_q(n, lattice, unit=1.0):
