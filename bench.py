@@ -349,7 +349,9 @@ def run_mf(args):
         t64, lat64, prof64, _, _, stages64 = timed(gen64, args.fp64_steps, 1, None, profile=True)
         t64 = max_over_ranks(t64)
         ms64 = t64 / args.fp64_steps
+        fp64_tf = ctx.fma_rate("f64")
         fp64 = {"value": world * npart / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64,
+                "fp64_fma_peak_tflops_measured": fp64_tf,
                 "speedup_fp32_bulk_vs_fp64": ms64 / ms_per_step,
                 "kernels": {k: {"ms_total": round(v[0], 2), "launches": v[1]} for k, v in prof64.items()},
                 "stages_ms": stages64}

@@ -76,6 +76,10 @@ int mf_ctx_launch_counts(const mf_ctx* ctx, int64_t* counts, int n);
 int mf_ctx_profile(mf_ctx* ctx, int enable);
 /* sum of profiled device milliseconds and launch counts per kind; clears */
 int mf_ctx_profile_read(mf_ctx* ctx, double* ms, int64_t* counts, int n);
+/* measured FMA throughput of the device in TFLOP/s (prec MF_PREC_F64 or
+ * MF_PREC_F32), the arithmetic ceiling of the FP64 path's roofline (no
+ * reference counterpart) */
+int mf_probe_fma_rate(mf_ctx* ctx, int prec, double* tflops);
 /* page-locked host memory for streaming transfers (no reference counterpart) */
 int mf_host_alloc(size_t bytes, void** out);
 int mf_host_free(void* p);

@@ -61,6 +61,12 @@ class Context:
         _check(self.ptr, lib().mf_ctx_launch_counts(self.ptr, a.ctypes.data, 8))
         return dict(zip(self.KERNEL_KINDS, a.tolist()))
 
+    def fma_rate(self, prec: str = "f64") -> float:
+        """measured FMA throughput in TFLOP/s"""
+        r = C.c_double()
+        _check(self.ptr, lib().mf_probe_fma_rate(self.ptr, _PREC[prec], C.byref(r)))
+        return r.value
+
     def profile(self, enable: bool):
         _check(self.ptr, lib().mf_ctx_profile(self.ptr, int(enable)))
 

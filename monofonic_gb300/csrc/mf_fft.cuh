@@ -245,5 +245,8 @@ struct LineFFT {
 };
 
 struct SyncBlock { __device__ __forceinline__ void operator()() const { __syncthreads(); } };
+// all lanes of a warp run the same line-group code path, so a full-mask
+// warp barrier suffices when every line's threads sit inside one warp
+struct SyncWarp { __device__ __forceinline__ void operator()() const { __syncwarp(); } };
 
 }  // namespace mf

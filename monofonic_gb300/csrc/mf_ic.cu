@@ -63,99 +63,49 @@ __global__ void k_phi1(cplx<T>* wn, cplx<T>* phi, int n, double kfac, const doub
   }
 }
 
-struct AssembleArgs {
-  const void* phi;
-  const void* phi2;
-  const void* phi3;
-  const void* A3[3];
-  int order;
-  int d;          // component
-  double w1, w2, w3, w3c;  // g_n (positions) or vfac_n g_n (velocities) and the A3 weight
-  double unit_over_L;
-  int shift;      // multiply by exp(i s.k dx)
-  double s[3];
-  double dx;
-};
-
-// k-space displacement/velocity combination (ic_generator.cc:829-858,
-// :884-931) with the growth-factor-weighted order sum in FP64, times
-// unit/L, zero DC; optional sub-lattice phase of shift_field
-// (grid_fft.hh:832-842) folded in
+// growth-factor-weighted sum of the orders (ic_generator.cc:550-563 and
+// :835-845 / :889-899) in FP64, stored in the grid precision
 template <typename T>
-__global__ void k_assemble(AssembleArgs a, cplx<T>* out, int n, double kfac) {
-  const int Kz = n / 2 + 1;
-  const size_t tot = (size_t)n * n * Kz;
-  const cplx<T>* P1 = (const cplx<T>*)a.phi;
-  const cplx<T>* P2 = (const cplx<T>*)a.phi2;
-  const cplx<T>* P3 = (const cplx<T>*)a.phi3;
-  const int dp = (a.d + 1) % 3, dpp = (a.d + 2) % 3;
-  const cplx<T>* Adp = (const cplx<T>*)a.A3[dp];
-  const cplx<T>* Adpp = (const cplx<T>*)a.A3[dpp];
+__global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, const cplx<T>* p3, size_t tot,
+                         double w1, double w2, double w3) {
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
-    const int kz = (int)(idx % Kz);
-    const int j = (int)((idx / Kz) % n);
-    const int i = (int)(idx / ((size_t)Kz * n));
-    const int ijk[3] = {i, j, kz};
-    const double gd = gradk<double>(ijk[a.d], n, kfac);
-    cplx<T> v = P1[idx];
-    double tr = a.w1 * (double)v.x, ti = a.w1 * (double)v.y;
-    if (a.order > 1) {
-      v = P2[idx];
-      tr += a.w2 * (double)v.x;
-      ti += a.w2 * (double)v.y;
-    }
-    if (a.order > 2) {
-      v = P3[idx];
-      tr += a.w3 * (double)v.x;
-      ti += a.w3 * (double)v.y;
-    }
-    // i g_d * phitot
-    double rr = -gd * ti, ri = gd * tr;
-    if (a.order > 2) {
-      const double gp = gradk<double>(ijk[dp], n, kfac), gpp = gradk<double>(ijk[dpp], n, kfac);
-      const cplx<T> x1 = Adpp[idx], x2 = Adp[idx];
-      // i g_p A3[pp] - i g_pp A3[p], A3 scaled by w3c
-      const double ar = a.w3c * (-(gp * (double)x1.y) + gpp * (double)x2.y);
-      const double ai = a.w3c * (gp * (double)x1.x - gpp * (double)x2.x);
-      rr += ar;
-      ri += ai;
-    }
-    rr *= a.unit_over_L;
-    ri *= a.unit_over_L;
-    if (idx == 0) { rr = 0; ri = 0; }
-    if (a.shift) {
-      const double sh = a.s[0] * kcomp<double>(i, n, kfac) * a.dx + a.s[1] * kcomp<double>(j, n, kfac) * a.dx +
-                        a.s[2] * kcomp<double>(kz, n, kfac) * a.dx;
-      double sn, cs;
-      sincos(sh, &sn, &cs);
-      const double nr = rr * cs - ri * sn, ni = rr * sn + ri * cs;
-      rr = nr;
-      ri = ni;
-    }
-    out[idx] = mkc<T>(T(rr), T(ri));
+    const cplx<T> a = p1[idx];
+    double r = w1 * (double)a.x, im = w1 * (double)a.y;
+    if (p2) { const cplx<T> b = p2[idx]; r += w2 * (double)b.x; im += w2 * (double)b.y; }
+    if (p3) { const cplx<T> c = p3[idx]; r += w3 * (double)c.x; im += w3 * (double)c.y; }
+    out[idx] = mkc<T>(T(r), T(im));
   }
 }
 
-// lattice readout (set_positions / set_velocities, particle_generator.hh:499-639)
+// lattice readout of the three components of one sub-lattice
+// (set_positions / set_velocities, particle_generator.hh:499-639): particle
+// ip = ishift*n^3 + cell, AoS [ip][3]; positions q + Psi in FP64 with
+// q_d = (idx_d + s_d)/n * lunit (get_unit_r_shifted, grid_fft.hh:242-252)
 template <typename T, typename P>
-__global__ void k_lattice(const T* psi, int n, P* dst, int d, int ishift, double sd, double lunit, int with_q,
-                          int fields_mode) {
+__global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P* dst, int ishift, double s0,
+                           double s1, double s2, double lunit, int with_q, int fields_mode) {
   const size_t n3 = (size_t)n * n * n;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n3; c += (size_t)gridDim.x * blockDim.x) {
     const size_t line = c / n;
     const int k = (int)(c % n);
-    const double v = (double)psi[line * (n + 2) + k];
+    const size_t off = line * (n + 2) + k;
+    double v0 = (double)psi0[off], v1 = (double)psi1[off], v2 = (double)psi2[off];
     if (fields_mode) {
-      dst[(size_t)d * n3 + c] = (P)v;
+      dst[c] = (P)v0;
+      dst[n3 + c] = (P)v1;
+      dst[2 * n3 + c] = (P)v2;
       continue;
     }
-    double out = v;
     if (with_q) {
       const int j = (int)(line % n), i = (int)(line / n);
-      const int idx = (d == 0) ? i : (d == 1) ? j : k;
-      out = ((double)idx + sd) / (double)n * lunit + v;
+      v0 += ((double)i + s0) / (double)n * lunit;
+      v1 += ((double)j + s1) / (double)n * lunit;
+      v2 += ((double)k + s2) / (double)n * lunit;
     }
-    dst[3 * ((size_t)ishift * n3 + c) + d] = (P)out;
+    P* o = dst + 3 * ((size_t)ishift * n3 + c);
+    o[0] = (P)v0;
+    o[1] = (P)v1;
+    o[2] = (P)v2;
   }
 }
 
@@ -184,7 +134,8 @@ struct mf_ic {
   mf_ic_params p{};
   mf_grid* wn = nullptr;
   mf_grid* f[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // phi, phi2, phi3, A3x, A3y, A3z
-  mf_grid* tmp = nullptr;
+  mf_grid* tmp[3] = {nullptr, nullptr, nullptr};  // real-space components of one sub-lattice
+  void* phase = nullptr;  // exp(+2 pi i m / 2n), m in [0, 2n), grid precision
   mf_conv* conv = nullptr;
   double* amp = nullptr;
   int nk2 = 0;
@@ -352,48 +303,73 @@ int run_impl(mf_ic* ic, mf_particles* out) {
   const int overload = 1 << p.lattice;
   const bool fields = p.out_kind == MF_OUT_FIELDS;
 
-  AssembleArgs a{};
-  a.phi = ic->f[0]->d;
-  a.phi2 = ic->f[1] ? ic->f[1]->d : nullptr;
-  a.phi3 = ic->f[2] ? ic->f[2]->d : nullptr;
-  for (int d = 0; d < 3; ++d) a.A3[d] = ic->f[3 + d] ? ic->f[3 + d]->d : nullptr;
-  a.order = p.lpt_order;
-  a.dx = L / n;
-  T* tmpr = (T*)ic->tmp->d;
+  T* wsum = (T*)ic->wn->d;  // the noise grid is free after phi(1): holds the order sum
+  const cplx<T>* P1 = (const cplx<T>*)ic->f[0]->d;
+  const cplx<T>* P2 = ic->f[1] ? (const cplx<T>*)ic->f[1]->d : nullptr;
+  const cplx<T>* P3 = ic->f[2] ? (const cplx<T>*)ic->f[2]->d : nullptr;
+  const cplx<T>* twN = c->tw.get<T>(n, s);
+  const cplx<T>* twH = c->tw.get<T>(n / 2, s);
+  if (!twN || !twH) return set_err(c, MF_ERR_OOM, "twiddles");
+  const size_t n3 = (size_t)n * n * n;
   for (int pass = 0; pass < 2; ++pass) {  // 0: positions, 1: velocities
     const bool vel = pass == 1;
     // weights: positions g_n; velocities vfac_n g_n with vfac_n = n vfac
-    a.w1 = vel ? vf * g1 : g1;
-    a.w2 = vel ? 2 * vf * g2 : g2;
-    a.w3 = vel ? 3 * vf * g3 : g3;
-    a.w3c = vel ? 3 * vf * g3c : g3c;
-    a.unit_over_L = (vel ? p.vunit : p.lunit) / L;
+    const double w1 = vel ? vf * g1 : g1, w2 = vel ? 2 * vf * g2 : g2, w3 = vel ? 3 * vf * g3 : g3;
+    const double wA = vel ? 3 * vf * g3c : g3c;
+    {
+      LaunchScope ls(c, KK_POINTWISE);
+      k_phitot<T><<<blocks_for(nk), kThreads, 0, s>>>((cplx<T>*)wsum, P1, p.lpt_order > 1 ? P2 : nullptr,
+                                                     p.lpt_order > 2 ? P3 : nullptr, nk, w1, w2, w3);
+    }
+    CK(cudaGetLastError());
     void* dst = vel ? ic->dvel : ic->dpos;
-    for (int d = 0; d < 3; ++d) {
-      a.d = d;
-      for (int ish = 0; ish < overload; ++ish) {
-        a.shift = ish > 0;
-        for (int q = 0; q < 3; ++q) a.s[q] = kShifts[p.lattice][ish][q];
+    for (int ish = 0; ish < overload; ++ish) {
+      for (int d = 0; d < 3; ++d) {
+        T* tmpr = (T*)ic->tmp[d]->d;
+        cplx<T>* tk = (cplx<T>*)tmpr;
+        AssembleXInvOp<T> op{};
+        op.phitot = (const cplx<T>*)wsum;
+        op.A3p = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 1) % 3]->d : nullptr;
+        op.A3pp = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 2) % 3]->d : nullptr;
+        op.dst = tk;
+        op.phase = ish > 0 ? (const cplx<T>*)ic->phase : nullptr;
+        op.n = n;
+        op.Kz = Kz;
+        op.d = d;
+        op.s2x = (int)lround(2 * kShifts[p.lattice][ish][0]);
+        op.s2y = (int)lround(2 * kShifts[p.lattice][ish][1]);
+        op.s2z = (int)lround(2 * kShifts[p.lattice][ish][2]);
+        op.kfac = T(kfac);
+        op.wA = T(wA);
+        op.unit = T((vel ? p.vunit : p.lunit) / L);
         {
-          LaunchScope ls(c, KK_POINTWISE);
-          k_assemble<T><<<blocks_for(nk), kThreads, 0, s>>>(a, (cplx<T>*)tmpr, n, kfac);
+          LaunchScope ls(c, KK_FFT_COL);
+          CK(Launch<T>::assemble_xinv(n, op, n, Kz, twN, s));
         }
-        CK(cudaGetLastError());
-        CK(fft3d_c2r<T>(c, tmpr, n));
-        const size_t n3 = (size_t)n * n * n;
-        const double sd = kShifts[p.lattice][ish][d];
-        LaunchScope ls(c, KK_POINTWISE);
-        if (fields) {
-          k_lattice<T, double><<<blocks_for(n3), kThreads, 0, s>>>(tmpr, n, (double*)dst, d, 0, 0.0, 0.0, 0, 1);
-        } else if (p.pos64) {
-          k_lattice<T, double><<<blocks_for(n3), kThreads, 0, s>>>(tmpr, n, (double*)dst, d, ish, sd, p.lunit,
-                                                                  vel ? 0 : 1, 0);
-        } else {
-          k_lattice<T, float><<<blocks_for(n3), kThreads, 0, s>>>(tmpr, n, (float*)dst, d, ish, sd, p.lunit,
-                                                                 vel ? 0 : 1, 0);
+        {
+          LaunchScope ls(c, KK_FFT_COL);
+          CK(Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{tk, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s));
         }
-        CK(cudaGetLastError());
+        {
+          LaunchScope ls(c, KK_FFT_Z);
+          const T norm = T(1.0 / std::sqrt((double)n * (double)n * (double)n));
+          CK(Launch<T>::z_c2r_plain(n / 2, PlainZOp<T>{tmpr, n, norm}, n * n, Kz, twH, twN, s));
+        }
       }
+      const double* sh = kShifts[p.lattice][ish];
+      const T* q0 = (const T*)ic->tmp[0]->d;
+      const T* q1 = (const T*)ic->tmp[1]->d;
+      const T* q2 = (const T*)ic->tmp[2]->d;
+      LaunchScope ls(c, KK_POINTWISE);
+      if (fields)
+        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, 0, 0, 0, 0, 0, 0, 1);
+      else if (p.pos64)
+        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, ish, sh[0], sh[1], sh[2],
+                                                                  p.lunit, vel ? 0 : 1, 0);
+      else
+        k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, sh[0], sh[1], sh[2],
+                                                                 p.lunit, vel ? 0 : 1, 0);
+      CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ic->ev[5 + pass], s));
   }
@@ -470,7 +446,9 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   if (ic->wn) mf_grid_destroy(ic->wn);
   for (auto& g : ic->f)
     if (g) mf_grid_destroy(g);
-  if (ic->tmp) mf_grid_destroy(ic->tmp);
+  for (auto& g : ic->tmp)
+    if (g) mf_grid_destroy(g);
+  cudaFree(ic->phase);
   if (ic->conv) mf_conv_destroy(ic->conv);
   cudaFree(ic->amp);
   cudaFree(ic->dpos);
@@ -501,7 +479,33 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   const int nf = (p->lpt_order > 2) ? 6 : p->lpt_order;
   for (int i = 0; i < nf; ++i)
     if ((rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->f[i]))) return fail(rc);
-  if ((rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->tmp))) return fail(rc);
+  for (auto& g : ic->tmp)
+    if ((rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &g))) return fail(rc);
+  {
+    // sub-lattice phase table, generated on the host in extended precision
+    const long double pi = 3.141592653589793238462643383279502884L;
+    const size_t ps = (p->precision == MF_PREC_F32) ? sizeof(float2) : sizeof(double2);
+    std::vector<double> re(2 * n), im(2 * n);
+    for (int m = 0; m < 2 * n; ++m) {
+      const long double a = pi * (long double)m / (long double)n;
+      re[m] = (double)cosl(a);
+      im[m] = (double)sinl(a);
+      if ((2 * m) % n == 0) {  // exact on the axes
+        const int q = (2 * m) / n;
+        const double cq[4] = {1, 0, -1, 0}, sq[4] = {0, 1, 0, -1};
+        re[m] = cq[q];
+        im[m] = sq[q];
+      }
+    }
+    std::vector<unsigned char> h(ps * 2 * n);
+    for (int m = 0; m < 2 * n; ++m) {
+      if (p->precision == MF_PREC_F32) reinterpret_cast<float2*>(h.data())[m] = make_float2((float)re[m], (float)im[m]);
+      else reinterpret_cast<double2*>(h.data())[m] = make_double2(re[m], im[m]);
+    }
+    cudaError_t e2 = cudaMalloc(&ic->phase, h.size());
+    if (e2 == cudaSuccess) e2 = cudaMemcpy(ic->phase, h.data(), h.size(), cudaMemcpyHostToDevice);
+    if (e2 != cudaSuccess) return fail(cuda_err(c, e2, "mf_ic_create: phase table"));
+  }
   if (p->lpt_order > 1)
     if ((rc = mf_conv_create(c, n, p->boxlen, p->precision, p->convolver, &ic->conv))) return fail(rc);
   ic->nk2 = 3 * (n / 2) * (n / 2) + 1;

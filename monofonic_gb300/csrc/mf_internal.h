@@ -52,6 +52,8 @@ struct Launch {
   // strided pass kinds
   static cudaError_t colfft_plain(int L, bool inv, PlainStridedOp<T> op, int nslab, int ncols,
                                   const cplx<T>* tw, cudaStream_t s);
+  static cudaError_t assemble_xinv(int L, AssembleXInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                   cudaStream_t s);
   static cudaError_t conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
                                const cplx<T>* tw, cudaStream_t s);
   static cudaError_t conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,

@@ -39,10 +39,21 @@ k_colfft(OP op, const cplx<T>* __restrict__ tw, int ncols) {
     const int e = F::in_index(t, s);
     v[s] = valid ? op.load(slab, e, col) : mkc<T>(T(0), T(0));
   }
-  F::run(v, t, sm + c, NCOL, tw, SyncBlock{});
-  if (valid) {
+  if constexpr (OP::kPrefetch) {
+    C pre[F::E];
 #pragma unroll
-    for (int s = 0; s < F::E; ++s) op.store(slab, F::out_index(t, s), col, v[s]);
+    for (int s = 0; s < F::E; ++s) pre[s] = valid ? op.prefetch(slab, F::out_index(t, s), col) : mkc<T>(T(0), T(0));
+    F::run(v, t, sm + c, NCOL, tw, SyncBlock{});
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) op.store_pre(slab, F::out_index(t, s), col, v[s], pre[s]);
+    }
+  } else {
+    F::run(v, t, sm + c, NCOL, tw, SyncBlock{});
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) op.store(slab, F::out_index(t, s), col, v[s]);
+    }
   }
 }
 
@@ -124,46 +135,70 @@ __global__ void __launch_bounds__(NT) k_zc2r(OP op, const cplx<T>* __restrict__ 
 // the real values, r2c of the product, store of kz in [0, kout)
 // ---------------------------------------------------------------------------
 
-template <typename T, int H, int NT>
-__global__ void __launch_bounds__(NT) k_zconv(ZConvArgs<T> a, const cplx<T>* __restrict__ twH,
+// c2r pre-processing read straight from global memory: Z[k] = E + i O with
+// A = X[k], B = conj(X[H-k]) (zero for kz >= kin), imaginary parts of the
+// kz = 0 and kz = H terms dropped (FFTW's c2r convention)
+template <typename T, int H>
+__device__ __forceinline__ cplx<T> c2r_pre_g(const cplx<T>* __restrict__ src, int k, int kin,
+                                             const cplx<T>* __restrict__ twM) {
+  using C = cplx<T>;
+  C A = (k < kin) ? src[k] : mkc<T>(T(0), T(0));
+  C B = (H - k < kin) ? src[H - k] : mkc<T>(T(0), T(0));
+  if (k == 0) { A.y = T(0); B.y = T(0); }
+  B = cconj(B);
+  const C Ev = cadd(A, B);
+  const C Ov = cmulc(csub(A, B), twM[k]);
+  return mkc<T>(Ev.x - Ov.y, Ev.y + Ov.x);
+}
+
+// One thread group of TPL threads per line; when TPL divides 32 every line
+// lives inside one warp and all exchanges use warp barriers only.  The
+// operands' inverse transforms read their inputs straight from HBM, the
+// running product stays in registers, and only the final r2c
+// post-processing goes through shared memory once more.
+template <typename T, int H, int MAXR, int NT, int MINB, class SYNC>
+__global__ void __launch_bounds__(NT, MINB) k_zconv(ZConvArgs<T> a, const cplx<T>* __restrict__ twH,
                                                 const cplx<T>* __restrict__ twM) {
-  using FI = LineFFT<T, H, true>;
-  using FF = LineFFT<T, H, false>;
+  using FI = LineFFT<T, H, true, MAXR>;
+  using FF = LineFFT<T, H, false, MAXR>;
   static_assert(FI::E == FF::E && FI::TPL == FF::TPL, "plan mismatch");
   using C = cplx<T>;
-  constexpr int E = FI::E, TPL = FI::TPL;
+  constexpr int E = FI::E, TPL = FI::TPL, LPB = NT / TPL;
+  constexpr int LSTRIDE = H + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int t = threadIdx.x, ly = threadIdx.y;
-  const int line = blockIdx.x * blockDim.y + ly;
+  const int t = threadIdx.x % TPL, ly = threadIdx.x / TPL;
+  const int line = blockIdx.x * LPB + ly;
   const bool valid = line < a.nlines;
-  C* sm = reinterpret_cast<C*>(smem_raw) + ly * (2 * H + 2);
-  C* prod = sm + (H + 1);  // per-thread-owned slots of the running product
-  C v[E];
+  C* sm = reinterpret_cast<C*>(smem_raw) + ly * LSTRIDE;
+  SYNC sync;
+  C v[E], prod[E];
   for (int op = 0; op < a.nop; ++op) {
-    __syncthreads();
-    const C* src = a.in[op] + (long long)line * a.in_stride;
-    for (int k = t; k <= H; k += TPL) sm[k] = (valid && k < a.kin) ? src[k] : mkc<T>(T(0), T(0));
-    __syncthreads();
+    const C* base = (op == 0) ? a.in[0] : ((op == 1) ? a.in[1] : a.in[2]);
+    const C* src = base + (long long)(valid ? line : 0) * a.in_stride;
+    const int kin = valid ? a.kin : 0;
 #pragma unroll
-    for (int s = 0; s < E; ++s) v[s] = c2r_pre<T, H>(sm, FI::in_index(t, s), twM);
-    FI::run(v, t, sm, 1, twH, SyncBlock{});
-    // v[s] = (x[2m], x[2m+1]) with m = out_index(t, s); slots are thread-owned
+    for (int s = 0; s < E; ++s) v[s] = c2r_pre_g<T, H>(src, FI::in_index(t, s), kin, twM);
+    FI::run(v, t, sm, 1, twH, sync);
+    if (op == 0) {
 #pragma unroll
-    for (int s = 0; s < E; ++s) {
-      const int m = FI::out_index(t, s);
-      if (op == 0) prod[m] = v[s];
-      else { C p = prod[m]; p.x *= v[s].x; p.y *= v[s].y; prod[m] = p; }
+      for (int s = 0; s < E; ++s) prod[s] = v[s];
+    } else {
+#pragma unroll
+      for (int s = 0; s < E; ++s) { prod[s].x *= v[s].x; prod[s].y *= v[s].y; }
     }
   }
-  __syncthreads();
-  // forward transform of the packed product
+  // forward transform of the packed product: one exchange into stage-0 order
+  sync();
 #pragma unroll
-  for (int s = 0; s < E; ++s) v[s] = prod[FF::in_index(t, s)];
-  FF::run(v, t, sm, 1, twH, SyncBlock{});
-  __syncthreads();
+  for (int s = 0; s < E; ++s) sm[FI::out_index(t, s)] = prod[s];
+  sync();
+#pragma unroll
+  for (int s = 0; s < E; ++s) v[s] = sm[FF::in_index(t, s)];
+  FF::run(v, t, sm, 1, twH, sync);
+  sync();
 #pragma unroll
   for (int s = 0; s < E; ++s) sm[FF::out_index(t, s)] = v[s];
-  __syncthreads();
+  sync();
   if (valid) {
     C* dst = a.out + (long long)line * a.out_stride;
     for (int k = t; k < a.kout; k += TPL) {

@@ -4,6 +4,13 @@
 #pragma once
 
 #include "mf_internal.h"
+#include <type_traits>
+
+// CTAs per SM the fused z pass is compiled for in FP32 (a build-time knob)
+#ifndef MF_ZCONV_MINB_F32
+#define MF_ZCONV_MINB_F32 2
+#endif
+
 #include "mf_kernels.cuh"
 
 namespace mf {
@@ -74,16 +81,22 @@ cudaError_t launch_zc2r(OP op, int nlines, int kin, const cplx<T>* twH, const cp
   return cudaGetLastError();
 }
 
+// fused z pass: radix-4 plan (fewer registers per thread); 256 threads per
+// CTA; warp barriers when a line's threads fit in one warp
 template <typename T, int H>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
-  constexpr int LPB = z_lpb<T, H, 2 * H + 2>();
-  constexpr int TPL = LineFFT<T, H, true>::TPL;
-  const size_t smem = (size_t)LPB * (2 * H + 2) * sizeof(cplx<T>);
-  auto kern = k_zconv<T, H, TPL * LPB>;
+  constexpr int MAXR = 4;
+  constexpr int TPL = LineFFT<T, H, true, MAXR>::TPL;
+  constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
+  constexpr int NT = (TPL >= 256) ? TPL : (256 / TPL) * TPL;
+  constexpr int LPB = NT / TPL;
+  const size_t smem = (size_t)LPB * (H + 1) * sizeof(cplx<T>);
+  using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
+  constexpr int MINB = (sizeof(T) == 4) ? MF_ZCONV_MINB_F32 : 1;
+  auto kern = k_zconv<T, H, MAXR, NT, MINB, SYNC>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  dim3 block(TPL, LPB), grid((a.nlines + LPB - 1) / LPB);
-  kern<<<grid, block, smem, s>>>(a, twH, twM);
+  kern<<<(a.nlines + LPB - 1) / LPB, NT, smem, s>>>(a, twH, twM);
   return cudaGetLastError();
 }
 
@@ -121,7 +134,15 @@ cudaError_t Launch<T>::z_c2r_plain(int H, PlainZOp<T> op, int nlines, int kin, c
   switch (H) { MF_LEN_NH(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T>
+cudaError_t Launch<T>::assemble_xinv(int L, AssembleXInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                     cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s);
+  switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
 template cudaError_t Launch<MF_T>::colfft_plain(int, bool, PlainStridedOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::assemble_xinv(int, AssembleXInvOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_r2c_plain(int, PlainZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_c2r_plain(int, PlainZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 #endif

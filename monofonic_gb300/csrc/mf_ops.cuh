@@ -43,20 +43,22 @@ struct Operand {
   int d[4];
 };
 
+__device__ __forceinline__ int sel3(int d, int i, int j, int k) { return d == 0 ? i : (d == 1 ? j : k); }
+
 // apply the operand's k-space factor to f at (i, j, kz)
 template <typename T>
-__device__ __forceinline__ cplx<T> operand_value(const Operand<T>& o, cplx<T> f, int i, int j, int kz, int n, T kfac) {
-  if (o.kind == OPND_PLAIN) return f;
-  const int ijk[3] = {i, j, kz};
-  if (o.kind == OPND_GRAD) {
-    const T g = gradk<T>(ijk[o.d[0]], n, kfac);
+__device__ __forceinline__ cplx<T> operand_value(int kind, int d0, int d1, int d2, int d3, cplx<T> f, int i, int j,
+                                                int kz, int n, T kfac) {
+  if (kind == OPND_PLAIN) return f;
+  if (kind == OPND_GRAD) {
+    const T g = gradk<T>(sel3(d0, i, j, kz), n, kfac);
     return mkc<T>(-g * f.y, g * f.x);
   }
-  const T h1 = -(gradk<T>(ijk[o.d[0]], n, kfac) * gradk<T>(ijk[o.d[1]], n, kfac));
+  const T h1 = -(gradk<T>(sel3(d0, i, j, kz), n, kfac) * gradk<T>(sel3(d1, i, j, kz), n, kfac));
   T h = h1;
-  if (o.kind != OPND_HESS) {
-    const T h2 = -(gradk<T>(ijk[o.d[2]], n, kfac) * gradk<T>(ijk[o.d[3]], n, kfac));
-    h = (o.kind == OPND_SUM) ? (h1 + h2) : (h1 - h2);
+  if (kind != OPND_HESS) {
+    const T h2 = -(gradk<T>(sel3(d2, i, j, kz), n, kfac) * gradk<T>(sel3(d3, i, j, kz), n, kfac));
+    h = (kind == OPND_SUM) ? (h1 + h2) : (h1 - h2);
   }
   return mkc<T>(h * f.x, h * f.y);
 }
@@ -86,16 +88,26 @@ struct ConvXInvOp {
   C* dst[3];  // work buffers [M][M][Kz]; rows j < N of each x slab
   ConvGeom g;
   T kfac, scale;
+  static constexpr bool kPrefetch = false;
+  // operand fields selected without dynamic indexing (keeps them in registers)
+  template <int F>
+  __device__ __forceinline__ int dsel(int z) const {
+    return z == 0 ? opnd[0].d[F] : (z == 1 ? opnd[1].d[F] : opnd[2].d[F]);
+  }
   __device__ __forceinline__ C load(int j, int x, int kz) const {
     const int i = g.src_row(x);
     if (i < 0) return mkc<T>(T(0), T(0));
-    const Operand<T>& o = opnd[blockIdx.z];
-    const C f = o.f[((long long)i * g.N + j) * g.Kz + kz];
-    const C v = operand_value<T>(o, f, i, j, kz, g.N, kfac);
+    const int z = blockIdx.z;
+    const C* f = z == 0 ? opnd[0].f : (z == 1 ? opnd[1].f : opnd[2].f);
+    const int kind = z == 0 ? opnd[0].kind : (z == 1 ? opnd[1].kind : opnd[2].kind);
+    const C v0 = f[((long long)i * g.N + j) * g.Kz + kz];
+    const C v = operand_value<T>(kind, dsel<0>(z), dsel<1>(z), dsel<2>(z), dsel<3>(z), v0, i, j, kz, g.N, kfac);
     return mkc<T>(v.x * scale, v.y * scale);
   }
   __device__ __forceinline__ void store(int j, int x, int kz, C v) const {
-    dst[blockIdx.z][((long long)x * g.M + j) * g.Kz + kz] = v;
+    const int z = blockIdx.z;
+    C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
+    d[((long long)x * g.M + j) * g.Kz + kz] = v;
   }
 };
 
@@ -106,13 +118,18 @@ struct ConvYInvOp {
   const C* src[3];  // work buffers, compact rows j < N of each x slab
   C* dst[3];        // same buffers, rows y < M (in place per slab)
   ConvGeom g;
+  static constexpr bool kPrefetch = false;
   __device__ __forceinline__ C load(int x, int y, int kz) const {
     const int j = g.src_row(y);
     if (j < 0) return mkc<T>(T(0), T(0));
-    return src[blockIdx.z][((long long)x * g.M + j) * g.Kz + kz];
+    const int z = blockIdx.z;
+    const C* s = z == 0 ? src[0] : (z == 1 ? src[1] : src[2]);
+    return s[((long long)x * g.M + j) * g.Kz + kz];
   }
   __device__ __forceinline__ void store(int x, int y, int kz, C v) const {
-    dst[blockIdx.z][((long long)x * g.M + y) * g.Kz + kz] = v;
+    const int z = blockIdx.z;
+    C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
+    d[((long long)x * g.M + y) * g.Kz + kz] = v;
   }
 };
 
@@ -123,6 +140,7 @@ struct ConvYFwdOp {
   const C* src;  // work buffer, rows y < M
   C* dst;        // same buffer, compact rows j < N (in place per slab)
   ConvGeom g;
+  static constexpr bool kPrefetch = false;
   __device__ __forceinline__ C load(int x, int y, int kz) const {
     return src[((long long)x * g.M + y) * g.Kz + kz];
   }
@@ -145,24 +163,28 @@ struct ConvXFwdOp {
   T x;           // multiply_add_to factor
   int post_invlap;
   T kfac;
+  // the read-modify-write target is fetched before the transform so its
+  // latency overlaps the FFT
+  static constexpr bool kPrefetch = true;
   __device__ __forceinline__ C load(int j, int xx, int kz) const {
     return src[((long long)xx * g.M + j) * g.Kz + kz];
   }
-  __device__ __forceinline__ void store(int j, int xx, int kz, C v) const {
+  __device__ __forceinline__ C prefetch(int j, int xx, int kz) const {
+    const int i = g.kept_row(xx);
+    if (i < 0 || out_op == OUT_ASSIGN) return mkc<T>(T(0), T(0));
+    return target[((long long)i * g.N + j) * g.Kz + kz];
+  }
+  __device__ __forceinline__ void store_pre(int j, int xx, int kz, C v, C r) const {
     const int i = g.kept_row(xx);
     if (i < 0) return;
     const int nh = g.N >> 1;
     v = mkc<T>(v.x * scale, v.y * scale);
     if (g.orszag && (i == nh || j == nh || kz == nh)) v = mkc<T>(T(0), T(0));
     const long long idx = ((long long)i * g.N + j) * g.Kz + kz;
-    C r;
     if (out_op == OUT_ASSIGN) r = v;
-    else {
-      r = target[idx];
-      if (out_op == OUT_ADD) r = cadd(r, v);
-      else if (out_op == OUT_SUB) r = csub(r, v);
-      else r = mkc<T>(r.x + v.x * x, r.y + v.y * x);
-    }
+    else if (out_op == OUT_ADD) r = cadd(r, v);
+    else if (out_op == OUT_SUB) r = csub(r, v);
+    else r = mkc<T>(r.x + v.x * x, r.y + v.y * x);
     if (post_invlap) {
       const T kx = kcomp<T>(i, g.N, kfac), ky = kcomp<T>(j, g.N, kfac), kzz = kcomp<T>(kz, g.N, kfac);
       const T k2 = kx * kx + ky * ky + kzz * kzz;
@@ -170,6 +192,50 @@ struct ConvXFwdOp {
     }
     target[idx] = r;
   }
+  __device__ __forceinline__ void store(int j, int xx, int kz, C v) const { store_pre(j, xx, kz, v, prefetch(j, xx, kz)); }
+};
+
+// x pass of the c2r of one displacement / velocity component, with the
+// k-space assembly of ic_generator.cc:829-858 / :884-931 fused into the load:
+//   i g_d phitot + w_A (i g_d' A3[d''] - i g_d'' A3[d']), times unit/L, zero DC,
+// times the sub-lattice phase exp(i s.k dx) of shift_field (grid_fft.hh:832-842)
+// read from an exact table exp(+2 pi i m / 2n), m = sum_d 2 s_d k_d mod 2n.
+// slab = j, e = i, col = kz; in place on the destination grid.
+template <typename T>
+struct AssembleXInvOp {
+  using C = cplx<T>;
+  const C* phitot;  // growth-weighted order sum (FP64 sum stored in T)
+  const C* A3p;     // A3[d'] (nullptr below 3LPT)
+  const C* A3pp;    // A3[d'']
+  C* dst;
+  const C* phase;   // 2n entries, nullptr for the unshifted lattice
+  int n, Kz, d, s2x, s2y, s2z;
+  T kfac, wA, unit;
+  static constexpr bool kPrefetch = false;
+  __device__ __forceinline__ C load(int j, int i, int kz) const {
+    const long long idx = ((long long)i * n + j) * Kz + kz;
+    if (idx == 0) return mkc<T>(T(0), T(0));
+    const C P = phitot[idx];
+    const T gd = gradk<T>(sel3(d, i, j, kz), n, kfac);
+    T rr = -gd * P.y, ri = gd * P.x;
+    if (A3p) {
+      const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
+      const T gp = gradk<T>(sel3(dp, i, j, kz), n, kfac), gpp = gradk<T>(sel3(dpp, i, j, kz), n, kfac);
+      const C X1 = A3pp[idx], X2 = A3p[idx];
+      rr += wA * (-(gp * X1.y) + gpp * X2.y);
+      ri += wA * (gp * X1.x - gpp * X2.x);
+    }
+    rr *= unit;
+    ri *= unit;
+    if (phase) {
+      const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
+      int m = (s2x * ii + s2y * jj + s2z * kz) % (2 * n);
+      if (m < 0) m += 2 * n;
+      return cmul(mkc<T>(rr, ri), phase[m]);
+    }
+    return mkc<T>(rr, ri);
+  }
+  __device__ __forceinline__ void store(int j, int i, int kz, C v) const { dst[((long long)i * n + j) * Kz + kz] = v; }
 };
 
 // plain strided pass over an n-grid: element (slab, e, col) at
@@ -180,6 +246,7 @@ struct PlainStridedOp {
   C* p;
   long long e_str, slab_str;
   T scale;
+  static constexpr bool kPrefetch = false;
   __device__ __forceinline__ C load(int slab, int e, int col) const {
     return p[(long long)slab * slab_str + (long long)e * e_str + col];
   }

@@ -150,3 +150,54 @@ INST(double)
 #undef INST
 
 }  // namespace mf
+
+// ---------------------------------------------------------------------------
+// FMA-rate probe: 8 independent FMA chains per thread, used to measure the
+// FP64 (and FP32) arithmetic ceiling of the device the pipeline runs on
+// ---------------------------------------------------------------------------
+namespace {
+template <typename T>
+__global__ void k_fma_probe(T* out, int iters, T a, T b) {
+  T x0 = T(threadIdx.x) * T(1e-3), x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+  T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const T r = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (r == T(-12345.678)) out[0] = r;  // keeps the chains live
+}
+}  // namespace
+
+extern "C" int mf_probe_fma_rate(mf_ctx* c, int prec, double* tflops) {
+  if (!c || !tflops) return MF_ERR_ARG;
+  cudaSetDevice(c->device);
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const int blocks = nsm * 8, threads = 256, iters = (prec == MF_PREC_F64) ? 2048 : 65536;
+  void* out = nullptr;
+  cudaEvent_t e0, e1;
+  if (cudaMalloc(&out, 16) != cudaSuccess) return MF_ERR_OOM;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0, c->stream);
+    if (prec == MF_PREC_F64)
+      k_fma_probe<double><<<blocks, threads, 0, c->stream>>>((double*)out, iters, 0.999999, 1e-7);
+    else
+      k_fma_probe<float><<<blocks, threads, 0, c->stream>>>((float*)out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1, c->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return mf::cuda_err(c, e, "mf_probe_fma_rate");
+  *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+  return MF_OK;
+}
