@@ -22,6 +22,19 @@ int cuda_err(mf_ctx* c, cudaError_t e, const char* where) {
   return set_err(c, code, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+int check_device_error(mf_ctx* c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "stream synchronize");
+  int flag = 0;
+  e = cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_err(c, e, "device error flag");
+  if (flag) {
+    cudaMemset(c->d_err, 0, sizeof(int));
+    return set_err(c, ST_ERR_TIMEOUT, "a bounded device wait ran out (asynchronous copy did not complete)");
+  }
+  return ST_OK;
+}
+
 LaunchScope::LaunchScope(mf_ctx* c, int kind) : c_(c), kind_(kind) {
   ++c_->launches[kind];
   if (c_->profile) {
@@ -239,6 +252,7 @@ cudaError_t conv_run(mf_conv* cv, const Operand<T>* ops, int nop, cplx<T>* targe
   za.out_stride = Kz;
   za.nlines = M * M;
   za.out_scale = T(1);
+  za.err = c->d_err;
   {
     LaunchScope ls(c, KK_CONV_Z);
     e = Launch<T>::z_conv(H, za, twH, twM, s);
@@ -293,6 +307,11 @@ extern "C" int mf_ctx_create(int device, mf_ctx** out) {
     delete c;
     return MF_ERR_CUDA;
   }
+  if (cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return MF_ERR_CUDA;
+  }
   *out = c;
   return MF_OK;
 }
@@ -306,6 +325,7 @@ extern "C" int mf_ctx_destroy(mf_ctx* c) {
   c->tw.release();
   for (auto& rec : c->prof_events) { cudaEventDestroy(rec.second.first); cudaEventDestroy(rec.second.second); }
   for (auto e : c->event_pool) cudaEventDestroy(e);
+  cudaFree(c->d_err);
   cudaStreamDestroy(c->stream);
   delete c;
   return MF_OK;
@@ -315,7 +335,8 @@ extern "C" const char* mf_last_error(const mf_ctx* c) { return c ? c->err.c_str(
 
 extern "C" int mf_ctx_synchronize(mf_ctx* c) {
   if (!c) return MF_ERR_ARG;
-  return cuda_err(c, cudaStreamSynchronize(c->stream), "mf_ctx_synchronize");
+  cudaSetDevice(c->device);
+  return check_device_error(c);
 }
 
 // ---------------------------------------------------------------------------

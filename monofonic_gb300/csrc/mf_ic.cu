@@ -82,8 +82,8 @@ __global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, con
 // ip = ishift*n^3 + cell, AoS [ip][3]; positions q + Psi in FP64 with
 // q_d = (idx_d + s_d)/n * lunit (get_unit_r_shifted, grid_fft.hh:242-252)
 template <typename T, typename P>
-__global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P* dst, int ishift, double s0,
-                           double s1, double s2, double lunit, int with_q, int fields_mode) {
+__global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P* dst, int ishift,
+                           const double* __restrict__ q, int with_q, int fields_mode) {
   const size_t n3 = (size_t)n * n * n;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n3; c += (size_t)gridDim.x * blockDim.x) {
     const size_t line = c / n;
@@ -96,11 +96,11 @@ __global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P
       dst[2 * n3 + c] = (P)v2;
       continue;
     }
-    if (with_q) {
+    if (with_q) {  // q_d = (idx_d + s_d) / n * lunit, tabulated on the host
       const int j = (int)(line % n), i = (int)(line / n);
-      v0 += ((double)i + s0) / (double)n * lunit;
-      v1 += ((double)j + s1) / (double)n * lunit;
-      v2 += ((double)k + s2) / (double)n * lunit;
+      v0 = q[i] + v0;
+      v1 = q[n + j] + v1;
+      v2 = q[2 * n + k] + v2;
     }
     P* o = dst + 3 * ((size_t)ishift * n3 + c);
     o[0] = (P)v0;
@@ -136,6 +136,7 @@ struct mf_ic {
   mf_grid* f[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // phi, phi2, phi3, A3x, A3y, A3z
   mf_grid* tmp[3] = {nullptr, nullptr, nullptr};  // real-space components of one sub-lattice
   void* phase = nullptr;  // exp(+2 pi i m / 2n), m in [0, 2n), grid precision
+  double* qtab = nullptr; // lattice coordinates q[ishift][d][idx] * lunit
   mf_conv* conv = nullptr;
   double* amp = nullptr;
   int nk2 = 0;
@@ -356,19 +357,17 @@ int run_impl(mf_ic* ic, mf_particles* out) {
           CK(Launch<T>::z_c2r_plain(n / 2, PlainZOp<T>{tmpr, n, norm}, n * n, Kz, twH, twN, s));
         }
       }
-      const double* sh = kShifts[p.lattice][ish];
+      const double* qt = ic->qtab + (size_t)ish * 3 * n;
       const T* q0 = (const T*)ic->tmp[0]->d;
       const T* q1 = (const T*)ic->tmp[1]->d;
       const T* q2 = (const T*)ic->tmp[2]->d;
       LaunchScope ls(c, KK_POINTWISE);
       if (fields)
-        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, 0, 0, 0, 0, 0, 0, 1);
+        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, 0, qt, 0, 1);
       else if (p.pos64)
-        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, ish, sh[0], sh[1], sh[2],
-                                                                  p.lunit, vel ? 0 : 1, 0);
+        k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, ish, qt, vel ? 0 : 1, 0);
       else
-        k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, sh[0], sh[1], sh[2],
-                                                                 p.lunit, vel ? 0 : 1, 0);
+        k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, qt, vel ? 0 : 1, 0);
       CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ic->ev[5 + pass], s));
@@ -449,6 +448,7 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   for (auto& g : ic->tmp)
     if (g) mf_grid_destroy(g);
   cudaFree(ic->phase);
+  cudaFree(ic->qtab);
   if (ic->conv) mf_conv_destroy(ic->conv);
   cudaFree(ic->amp);
   cudaFree(ic->dpos);
@@ -505,6 +505,16 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     cudaError_t e2 = cudaMalloc(&ic->phase, h.size());
     if (e2 == cudaSuccess) e2 = cudaMemcpy(ic->phase, h.data(), h.size(), cudaMemcpyHostToDevice);
     if (e2 != cudaSuccess) return fail(cuda_err(c, e2, "mf_ic_create: phase table"));
+    // lattice coordinates (get_unit_r_shifted, grid_fft.hh:242-252) times lunit
+    const int ov = 1 << p->lattice;
+    std::vector<double> q((size_t)ov * 3 * n);
+    for (int ish = 0; ish < ov; ++ish)
+      for (int d = 0; d < 3; ++d)
+        for (int i = 0; i < n; ++i)
+          q[((size_t)ish * 3 + d) * n + i] = ((double)i + kShifts[p->lattice][ish][d]) / (double)n * p->lunit;
+    e2 = cudaMalloc(&ic->qtab, q.size() * sizeof(double));
+    if (e2 == cudaSuccess) e2 = cudaMemcpy(ic->qtab, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e2 != cudaSuccess) return fail(cuda_err(c, e2, "mf_ic_create: lattice table"));
   }
   if (p->lpt_order > 1)
     if ((rc = mf_conv_create(c, n, p->boxlen, p->precision, p->convolver, &ic->conv))) return fail(rc);
@@ -551,8 +561,9 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
   if (!ic->noise_set) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
   cudaSetDevice(ic->ctx->device);
-  const int rc = (ic->p.precision == MF_PREC_F64) ? run_impl<double>(ic, out) : run_impl<float>(ic, out);
+  int rc = (ic->p.precision == MF_PREC_F64) ? run_impl<double>(ic, out) : run_impl<float>(ic, out);
   ic->noise_set = false;  // the noise grid is consumed (transformed and normalised in place)
+  if (rc == MF_OK) rc = check_device_error(ic->ctx);
   return rc;
 }
 

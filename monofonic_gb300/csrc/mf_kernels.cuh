@@ -14,6 +14,7 @@
 #pragma once
 
 #include "mf_fft.cuh"
+#include "mf_tma.cuh"
 
 namespace mf {
 
@@ -208,6 +209,114 @@ __global__ void __launch_bounds__(NT, MINB) k_zconv(ZConvArgs<T> a, const cplx<T
       const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
       dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-pipelined fused z pass.  Persistent CTAs walk batches of LPB
+// consecutive lines; the operands of the next batch are fetched by bulk
+// asynchronous copies (cp.async.bulk, one per operand, completion counted on
+// an mbarrier) into the other half of a double buffer while the current batch
+// is transformed, so HBM traffic overlaps the FFT work.
+// Shared memory: [2 mbarriers | stage[2][nop][LPB][kin] | exchange[LPB][H+1]]
+// ---------------------------------------------------------------------------
+template <typename T, int H>
+__device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin, const cplx<T>* __restrict__ twM) {
+  using C = cplx<T>;
+  C A = (k < kin) ? src[k] : mkc<T>(T(0), T(0));
+  C B = (H - k < kin) ? src[H - k] : mkc<T>(T(0), T(0));
+  if (k == 0) { A.y = T(0); B.y = T(0); }
+  B = cconj(B);
+  const C Ev = cadd(A, B);
+  const C Ov = cmulc(csub(A, B), twM[k]);
+  return mkc<T>(Ev.x - Ov.y, Ev.y + Ov.x);
+}
+
+template <typename T, int H, int MAXR, int LPB, class SYNC>
+__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL)
+k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
+  using FI = LineFFT<T, H, true, MAXR>;
+  using FF = LineFFT<T, H, false, MAXR>;
+  using C = cplx<T>;
+  constexpr int E = FI::E, TPL = FI::TPL;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+  const int nop = a.nop, kin = a.kin;
+  C* stage = reinterpret_cast<C*>(smem_raw + 128);
+  const int per_op = LPB * kin;
+  C* xchg = stage + 2 * nop * per_op;
+  const int t = threadIdx.x % TPL, ly = threadIdx.x / TPL;
+  C* sm = xchg + ly * (H + 1);
+  const int nbatch = a.nlines / LPB;
+  const unsigned bytes_op = (unsigned)(per_op * sizeof(C));
+  const C* in0 = a.in[0];
+  const C* in1 = a.in[1];
+  const C* in2 = a.in[2];
+  SYNC sync;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int b, int st) {
+    mbar_arrive_expect_tx(&bars[st], (unsigned)nop * bytes_op);
+    const long long off = (long long)b * per_op;
+    tma_load_1d(stage + (st * nop + 0) * per_op, in0 + off, bytes_op, &bars[st]);
+    if (nop > 1) tma_load_1d(stage + (st * nop + 1) * per_op, in1 + off, bytes_op, &bars[st]);
+    if (nop > 2) tma_load_1d(stage + (st * nop + 2) * per_op, in2 + off, bytes_op, &bars[st]);
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < nbatch) issue(blockIdx.x, 0);
+  int iter = 0;
+  bool pending_other = false;
+  for (int b = blockIdx.x; b < nbatch; b += gridDim.x, ++iter) {
+    const int st = iter & 1;
+    const int bn = b + gridDim.x;
+    if (threadIdx.x == 0 && bn < nbatch) {
+      fence_proxy_async_smem();
+      issue(bn, st ^ 1);
+    }
+    pending_other = bn < nbatch;
+    const bool ok = mbar_wait_bounded(&bars[st], (iter >> 1) & 1, a.err, 1);
+    if (!__syncthreads_and(ok)) {
+      // give the copy still in flight into the other buffer a bounded chance to land
+      if (pending_other) mbar_wait_bounded(&bars[st ^ 1], ((iter + 1) >> 1) & 1, nullptr, 0);
+      return;
+    }
+    C v[E], prod[E];
+    for (int op = 0; op < nop; ++op) {
+      const C* src = stage + (st * nop + op) * per_op + ly * kin;
+#pragma unroll
+      for (int s = 0; s < E; ++s) v[s] = c2r_pre_s<T, H>(src, FI::in_index(t, s), kin, twM);
+      FI::run(v, t, sm, 1, twH, sync);
+      if (op == 0) {
+#pragma unroll
+        for (int s = 0; s < E; ++s) prod[s] = v[s];
+      } else {
+#pragma unroll
+        for (int s = 0; s < E; ++s) { prod[s].x *= v[s].x; prod[s].y *= v[s].y; }
+      }
+    }
+    sync();
+#pragma unroll
+    for (int s = 0; s < E; ++s) sm[FI::out_index(t, s)] = prod[s];
+    sync();
+#pragma unroll
+    for (int s = 0; s < E; ++s) v[s] = sm[FF::in_index(t, s)];
+    FF::run(v, t, sm, 1, twH, sync);
+    sync();
+#pragma unroll
+    for (int s = 0; s < E; ++s) sm[FF::out_index(t, s)] = v[s];
+    sync();
+    C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
+    for (int k = t; k < a.kout; k += TPL) {
+      const C zk = sm[k % H];
+      const C zc = cconj(sm[(H - k) % H]);
+      const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
+      const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
+      dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);
+    }
+    __syncthreads();  // stage[st] fully consumed before it is refilled
   }
 }
 

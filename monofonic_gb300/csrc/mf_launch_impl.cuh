@@ -10,6 +10,10 @@
 #ifndef MF_ZCONV_MINB_F32
 #define MF_ZCONV_MINB_F32 2
 #endif
+// 1: TMA-pipelined fused z pass where the layout allows it (a build-time knob)
+#ifndef MF_ZCONV_TMA
+#define MF_ZCONV_TMA 1
+#endif
 
 #include "mf_kernels.cuh"
 
@@ -81,17 +85,52 @@ cudaError_t launch_zc2r(OP op, int nlines, int kin, const cplx<T>* twH, const cp
   return cudaGetLastError();
 }
 
-// fused z pass: radix-4 plan (fewer registers per thread); 256 threads per
-// CTA; warp barriers when a line's threads fit in one warp
+// lines per batch of the TMA z pass: a power of two >= 2 (so a batch of
+// FP32 lines of odd length is a multiple of 16 bytes), ~256 FP32 / ~128 FP64
+// threads per CTA
+template <typename T, int TPL>
+constexpr int tma_lines_per_batch() {
+  const int target = ((sizeof(T) == 4) ? 256 : 128) / TPL;
+  int l = 2;
+  while (l * 2 <= target) l *= 2;
+  return l;
+}
+
+// fused z pass: the TMA-pipelined persistent kernel when every batch of LPB
+// lines is one 16-byte aligned contiguous block per operand, otherwise the
+// direct-load kernel.  Radix-4 plan (fewer registers per thread); warp
+// barriers when a line's threads fit in one warp.
 template <typename T, int H>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
   constexpr int MAXR = 4;
   constexpr int TPL = LineFFT<T, H, true, MAXR>::TPL;
   constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
+  using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
+  constexpr int LPBT = tma_lines_per_batch<T, TPL>();
+  const bool tma_ok = MF_ZCONV_TMA && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
+                      (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
+                      ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
+                      (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
+  if (tma_ok) {
+    auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC>;
+    const size_t smem = 128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * (H + 1)) * sizeof(cplx<T>);
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LPBT * TPL, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int nbatch = a.nlines / LPBT;
+    int grid = nsm * per_sm;
+    if (grid > nbatch) grid = nbatch;
+    kern<<<grid, LPBT * TPL, smem, s>>>(a, twH, twM);
+    return cudaGetLastError();
+  }
   constexpr int NT = (TPL >= 256) ? TPL : (256 / TPL) * TPL;
   constexpr int LPB = NT / TPL;
   const size_t smem = (size_t)LPB * (H + 1) * sizeof(cplx<T>);
-  using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
   constexpr int MINB = (sizeof(T) == 4) ? MF_ZCONV_MINB_F32 : 1;
   auto kern = k_zconv<T, H, MAXR, NT, MINB, SYNC>;
   cudaError_t e = set_smem(kern, smem);

@@ -288,6 +288,7 @@ struct ZConvArgs {
   long long out_stride;
   int nlines;
   T out_scale;
+  int* err;               // device error flag (bounded waits), may be null
 };
 
 }  // namespace mf

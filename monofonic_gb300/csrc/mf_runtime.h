@@ -30,6 +30,7 @@ struct mf_ctx {
   mf::TwiddleCache tw;
   std::string err;
   int children = 0;  // live grids, convolvers and pipelines on this context
+  int* d_err = nullptr;  // device error flag set by bounded waits in kernels
   // launch accounting
   long long launches[mf::KK_COUNT] = {};
   bool profile = false;
@@ -77,6 +78,9 @@ struct mf_conv {
 namespace mf {
 
 int set_err(mf_ctx* c, int code, const std::string& msg);
+// synchronises the context's stream and turns a raised device error flag
+// (a bounded wait that ran out) into MF_ERR_TIMEOUT; clears the flag
+int check_device_error(mf_ctx* c);
 int cuda_err(mf_ctx* c, cudaError_t e, const char* where);
 
 inline size_t grid_reals(int n) { return (size_t)(n + 2) * n * n; }
