@@ -7,6 +7,7 @@ under monofonic_gb300/_build/ keyed on the source and header timestamps.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
 import shutil
 import subprocess
@@ -18,6 +19,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmfgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# extra compile definitions (tuning knobs such as -DMF_ZCONV_TMA_MAXR=4); a
+# different set builds into its own object directory
+EXTRA = os.environ.get("MF_NVCC_FLAGS", "").split()
 
 
 def _nvcc():
@@ -41,14 +45,20 @@ def _headers_mtime():
     return max(ts) if ts else 0.0
 
 
+def _objdir():
+    if not EXTRA:
+        return BUILD
+    return os.path.join(BUILD, hashlib.sha1(" ".join(EXTRA).encode()).hexdigest()[:10])
+
+
 def _compile(src, nvcc, hdr_t, verbose):
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    obj = os.path.join(_objdir(), os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), hdr_t):
         return obj, None
-    cmd = [nvcc, *ARCH, *FLAGS, "-c", path, "-o", obj]
+    cmd = [nvcc, *ARCH, *FLAGS, *EXTRA, "-c", path, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc, "-x", "cu", *ARCH, *FLAGS, "-c", path, "-o", obj]
+        cmd = [nvcc, "-x", "cu", *ARCH, *FLAGS, *EXTRA, "-c", path, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -58,7 +68,7 @@ def _compile(src, nvcc, hdr_t, verbose):
 
 
 def build(verbose: bool = False, jobs: int | None = None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(_objdir(), exist_ok=True)
     nvcc = _nvcc()
     hdr_t = _headers_mtime()
     srcs = _sources()
@@ -72,13 +82,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if errs:
         raise RuntimeError("libmfgpu build failed:\n" + "\n".join(errs))
     newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+    stamp = LIB + ".flags"
+    same_flags = os.path.exists(stamp) and open(stamp).read() == " ".join(EXTRA)
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest or not same_flags:
         tmp = LIB + ".tmp"
         cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("libmfgpu link failed:\n" + r.stdout + r.stderr)
         os.replace(tmp, LIB)
+        with open(stamp, "w") as f:
+            f.write(" ".join(EXTRA))
     return LIB
 
 

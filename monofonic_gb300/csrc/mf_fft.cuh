@@ -152,8 +152,16 @@ __host__ __device__ constexpr int plan_lcur(int L, int maxr, int s) {
   int p = 1; for (int i = 0; i < s; ++i) p *= plan_radix(L, maxr, i); return p;
 }
 
-// Line FFT of length L in precision T, direction INV, radices up to MAXR.
-template <typename T, int L, bool INV, int MAXR = 8>
+// padded shared-memory index: one spare element per 16 (128 B of float2),
+// which makes every exchange of a radix-8-first plan free of bank conflicts
+// when a line's elements are contiguous in shared memory (stride 1)
+template <bool PAD>
+__device__ __forceinline__ int pidx(int e) { return PAD ? e + (e >> 4) : e; }
+__host__ __device__ constexpr int padded_len(int L, bool pad) { return pad ? L + (L >> 4) + 1 : L; }
+
+// Line FFT of length L in precision T, direction INV, radices up to MAXR;
+// PAD selects the padded shared-memory index for contiguous (stride-1) lines.
+template <typename T, int L, bool INV, int MAXR = 8, bool PAD = false>
 struct LineFFT {
   static_assert(plan_ok(L), "FFT length must be 2^a 3^b >= 4");
   using C = cplx<T>;
@@ -205,7 +213,7 @@ struct LineFFT {
       const int k = b % LC;
       const int base = (b - k) * R + k;
 #pragma unroll
-      for (int q = 0; q < R; ++q) sm[(base + q * LC) * cs] = v[m * R + q];
+      for (int q = 0; q < R; ++q) sm[pidx<PAD>(base + q * LC) * cs] = v[m * R + q];
     }
   }
 
@@ -218,7 +226,7 @@ struct LineFFT {
     for (int m = 0; m < NB; ++m) {
       const int b = t + m * TPL;
 #pragma unroll
-      for (int p = 0; p < R; ++p) v[m * R + p] = sm[(b + p * (L / R)) * cs];
+      for (int p = 0; p < R; ++p) v[m * R + p] = sm[pidx<PAD>(b + p * (L / R)) * cs];
     }
   }
 

@@ -233,12 +233,13 @@ __device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin,
 }
 
 template <typename T, int H, int MAXR, int LPB, class SYNC>
-__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL)
+__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR, true>::TPL)
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
-  using FI = LineFFT<T, H, true, MAXR>;
-  using FF = LineFFT<T, H, false, MAXR>;
+  using FI = LineFFT<T, H, true, MAXR, true>;
+  using FF = LineFFT<T, H, false, MAXR, true>;
   using C = cplx<T>;
   constexpr int E = FI::E, TPL = FI::TPL;
+  constexpr int LS = padded_len(H, true);  // padded per-line exchange length
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
   const int nop = a.nop, kin = a.kin;
@@ -246,7 +247,7 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
   const int per_op = LPB * kin;
   C* xchg = stage + 2 * nop * per_op;
   const int t = threadIdx.x % TPL, ly = threadIdx.x / TPL;
-  C* sm = xchg + ly * (H + 1);
+  C* sm = xchg + ly * LS;
   const int nbatch = a.nlines / LPB;
   const unsigned bytes_op = (unsigned)(per_op * sizeof(C));
   const C* in0 = a.in[0];
@@ -299,19 +300,19 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
     }
     sync();
 #pragma unroll
-    for (int s = 0; s < E; ++s) sm[FI::out_index(t, s)] = prod[s];
+    for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
     sync();
 #pragma unroll
-    for (int s = 0; s < E; ++s) v[s] = sm[FF::in_index(t, s)];
+    for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
     FF::run(v, t, sm, 1, twH, sync);
     sync();
 #pragma unroll
-    for (int s = 0; s < E; ++s) sm[FF::out_index(t, s)] = v[s];
+    for (int s = 0; s < E; ++s) sm[pidx<true>(FF::out_index(t, s))] = v[s];
     sync();
     C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
     for (int k = t; k < a.kout; k += TPL) {
-      const C zk = sm[k % H];
-      const C zc = cconj(sm[(H - k) % H]);
+      const C zk = sm[pidx<true>(k % H)];
+      const C zc = cconj(sm[pidx<true>((H - k) % H)]);
       const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
       const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
       dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);

@@ -14,6 +14,10 @@
 #ifndef MF_ZCONV_TMA
 #define MF_ZCONV_TMA 1
 #endif
+// largest radix of the TMA z pass plan (8: fewer exchanges, more registers)
+#ifndef MF_ZCONV_TMA_MAXR
+#define MF_ZCONV_TMA_MAXR 8
+#endif
 
 #include "mf_kernels.cuh"
 
@@ -102,32 +106,41 @@ constexpr int tma_lines_per_batch() {
 // barriers when a line's threads fit in one warp.
 template <typename T, int H>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
+  {
+    // TMA path: radix-8-first plan with the padded (conflict-free) exchange layout
+    constexpr int MAXR = MF_ZCONV_TMA_MAXR;
+    constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
+    constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
+    using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
+    constexpr int LPBT = tma_lines_per_batch<T, TPL>();
+    const bool tma_ok = MF_ZCONV_TMA && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
+                        (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
+                        ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
+                        (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
+    if (tma_ok) {
+      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC>;
+      const size_t smem =
+          128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * padded_len(H, true)) * sizeof(cplx<T>);
+      cudaError_t e = set_smem(kern, smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, nsm = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LPBT * TPL, smem);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) per_sm = 1;
+      const int nbatch = a.nlines / LPBT;
+      int grid = nsm * per_sm;
+      if (grid > nbatch) grid = nbatch;
+      kern<<<grid, LPBT * TPL, smem, s>>>(a, twH, twM);
+      return cudaGetLastError();
+    }
+  }
+  // direct-load fallback: radix-4 plan, unpadded
   constexpr int MAXR = 4;
   constexpr int TPL = LineFFT<T, H, true, MAXR>::TPL;
   constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
   using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
-  constexpr int LPBT = tma_lines_per_batch<T, TPL>();
-  const bool tma_ok = MF_ZCONV_TMA && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
-                      (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
-                      ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
-                      (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
-  if (tma_ok) {
-    auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC>;
-    const size_t smem = 128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * (H + 1)) * sizeof(cplx<T>);
-    cudaError_t e = set_smem(kern, smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0, nsm = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LPBT * TPL, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const int nbatch = a.nlines / LPBT;
-    int grid = nsm * per_sm;
-    if (grid > nbatch) grid = nbatch;
-    kern<<<grid, LPBT * TPL, smem, s>>>(a, twH, twM);
-    return cudaGetLastError();
-  }
   constexpr int NT = (TPL >= 256) ? TPL : (256 / TPL) * TPL;
   constexpr int LPB = NT / TPL;
   const size_t smem = (size_t)LPB * (H + 1) * sizeof(cplx<T>);
