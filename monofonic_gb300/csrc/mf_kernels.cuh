@@ -59,6 +59,81 @@ k_colfft(OP op, const cplx<T>* __restrict__ tw, int ncols) {
 }
 
 // ---------------------------------------------------------------------------
+// persistent, double-buffered strided pass.  Each CTA walks tiles
+// (column tile, slab, operand) with stride gridDim.x; while a tile is being
+// transformed, the raw elements of the CTA's next tile are already being
+// copied into the other shared-memory buffer with cp.async.  Every thread
+// copies exactly the elements it reads for its first FFT stage, so a
+// per-thread wait_group suffices before the read.
+// OP: kPipe, srcp(z, slab, e, col) -> const C* (nullptr = zero),
+//     xform(z, slab, e, col, raw), store_z(z, slab, e, col, v)
+//     (+ kPrefetch: prefetch/store_pre on the same coordinates)
+// ---------------------------------------------------------------------------
+template <typename T, int L, bool INV, int NCOL, class OP>
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV>::TPL, (NCOL * LineFFT<T, L, INV>::TPL <= 256) ? 2 : 1)
+k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
+  using F = LineFFT<T, L, INV>;
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + L * NCOL;
+  const int c = threadIdx.x, t = threadIdx.y;
+  const int total = ntc * nslab * nz;
+  auto issue = [&](int tl, C* buf) {
+    const int ct = tl % ntc, r = tl / ntc, slab = r % nslab, z = r / nslab;
+    const int col = ct * NCOL + c;
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) {
+      const int e = F::in_index(t, s);
+      C* d = buf + e * NCOL + c;
+      const C* g = (col < ncols) ? op.srcp(z, slab, e, col) : nullptr;
+      if (g) {
+        if constexpr (sizeof(C) == 16) cp_async16(d, g); else cp_async8(d, g);
+      } else {
+        *d = mkc<T>(T(0), T(0));
+      }
+    }
+    cp_async_commit();
+  };
+  int tl = blockIdx.x;
+  if (tl < total) issue(tl, buf0); else cp_async_commit();
+  for (int it = 0; tl < total; tl += gridDim.x, ++it) {
+    C* cur = (it & 1) ? buf1 : buf0;
+    C* nxt = (it & 1) ? buf0 : buf1;
+    const int tn = tl + gridDim.x;
+    if (tn < total) issue(tn, nxt); else cp_async_commit();
+    cp_async_wait<1>();
+    const int ct = tl % ntc, r = tl / ntc, slab = r % nslab, z = r / nslab;
+    const int col = ct * NCOL + c;
+    const bool valid = col < ncols;
+    C v[F::E];
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) {
+      const int e = F::in_index(t, s);
+      v[s] = valid ? op.xform(z, slab, e, col, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+    }
+    if constexpr (OP::kPrefetch) {
+      C pre[F::E];
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) pre[s] = valid ? op.prefetch(slab, F::out_index(t, s), col) : mkc<T>(T(0), T(0));
+      F::run(v, t, cur + c, NCOL, tw, SyncBlock{});
+      if (valid) {
+#pragma unroll
+        for (int s = 0; s < F::E; ++s) op.store_pre(slab, F::out_index(t, s), col, v[s], pre[s]);
+      }
+    } else {
+      F::run(v, t, cur + c, NCOL, tw, SyncBlock{});
+      if (valid) {
+#pragma unroll
+        for (int s = 0; s < F::E; ++s) op.store_z(z, slab, F::out_index(t, s), col, v[s]);
+      }
+    }
+    __syncthreads();  // cur is refilled by the next iteration's copies
+  }
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // z pass, real -> half complex (forward), one line per thread group
 // OP: __device__ C load_pair(int line, int m) const;   // (x[2m], x[2m+1])
 //     __device__ void store(int line, int k, C v) const;  // k in [0, kout)

@@ -10,6 +10,10 @@
 #ifndef MF_ZCONV_MINB_F32
 #define MF_ZCONV_MINB_F32 2
 #endif
+// 1: persistent double-buffered (cp.async) strided passes (a build-time knob)
+#ifndef MF_COL_PIPE
+#define MF_COL_PIPE 1
+#endif
 // 1: TMA-pipelined fused z pass where the layout allows it (a build-time knob)
 #ifndef MF_ZCONV_TMA
 #define MF_ZCONV_TMA 1
@@ -50,17 +54,50 @@ inline cudaError_t set_smem(K kern, size_t smem) {
   return cudaSuccess;
 }
 
+// columns per CTA of the pipelined strided pass (two tile buffers): 64-byte
+// rows, at least 128 threads
+template <typename T, int L>
+constexpr int pipe_ncol() {
+  constexpr int tpl = LineFFT<T, L, false>::TPL;
+  int nc = (sizeof(T) == 4) ? 8 : 4;
+  while (nc * tpl > 1024) nc /= 2;
+  while (nc * tpl < 128 && nc < 32) nc *= 2;
+  return nc;
+}
+
 template <typename T, int L, bool INV, class OP>
 cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s) {
-  constexpr int NC = col_ncol<T, L>();
-  constexpr int TPL = LineFFT<T, L, INV>::TPL;
-  const size_t smem = (size_t)L * NC * sizeof(cplx<T>);
-  auto kern = k_colfft<T, L, INV, NC, OP>;
-  cudaError_t e = set_smem(kern, smem);
-  if (e != cudaSuccess) return e;
-  dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, nz);
-  kern<<<grid, block, smem, s>>>(op, tw, ncols);
-  return cudaGetLastError();
+  if constexpr (OP::kPipe && MF_COL_PIPE) {
+    constexpr int NC = pipe_ncol<T, L>();
+    constexpr int TPL = LineFFT<T, L, INV>::TPL;
+    const size_t smem = (size_t)2 * L * NC * sizeof(cplx<T>);
+    auto kern = k_colfft_pipe<T, L, INV, NC, OP>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NC * TPL, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int ntc = (ncols + NC - 1) / NC;
+    const int total = ntc * nslab * nz;
+    int grid = nsm * per_sm;
+    if (grid > total) grid = total;
+    dim3 block(NC, TPL);
+    kern<<<grid, block, smem, s>>>(op, tw, ncols, ntc, nslab, nz);
+    return cudaGetLastError();
+  } else {
+    constexpr int NC = col_ncol<T, L>();
+    constexpr int TPL = LineFFT<T, L, INV>::TPL;
+    const size_t smem = (size_t)L * NC * sizeof(cplx<T>);
+    auto kern = k_colfft<T, L, INV, NC, OP>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, nz);
+    kern<<<grid, block, smem, s>>>(op, tw, ncols);
+    return cudaGetLastError();
+  }
 }
 
 template <typename T, int H, class OP>

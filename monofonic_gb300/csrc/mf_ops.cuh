@@ -109,6 +109,24 @@ struct ConvXInvOp {
     C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
     d[((long long)x * g.M + j) * g.Kz + kz] = v;
   }
+  // pipelined form (k_colfft_pipe): raw source element and on-read transform; z = operand
+  static constexpr bool kPipe = true;
+  __device__ __forceinline__ const C* srcp(int z, int j, int x, int kz) const {
+    const int i = g.src_row(x);
+    if (i < 0) return nullptr;
+    const C* f = z == 0 ? opnd[0].f : (z == 1 ? opnd[1].f : opnd[2].f);
+    return f + ((long long)i * g.N + j) * g.Kz + kz;
+  }
+  __device__ __forceinline__ C xform(int z, int j, int x, int kz, C v0) const {
+    const int i = g.src_row(x);
+    const int kind = z == 0 ? opnd[0].kind : (z == 1 ? opnd[1].kind : opnd[2].kind);
+    const C v = operand_value<T>(kind, dsel<0>(z), dsel<1>(z), dsel<2>(z), dsel<3>(z), v0, i, j, kz, g.N, kfac);
+    return mkc<T>(v.x * scale, v.y * scale);
+  }
+  __device__ __forceinline__ void store_z(int z, int j, int x, int kz, C v) const {
+    C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
+    d[((long long)x * g.M + j) * g.Kz + kz] = v;
+  }
 };
 
 // y pass of the operands' c2r: slab = x in [0,M), e = y in [0,M), col = kz
@@ -131,6 +149,18 @@ struct ConvYInvOp {
     C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
     d[((long long)x * g.M + y) * g.Kz + kz] = v;
   }
+  static constexpr bool kPipe = true;
+  __device__ __forceinline__ const C* srcp(int z, int x, int y, int kz) const {
+    const int j = g.src_row(y);
+    if (j < 0) return nullptr;
+    const C* s0 = z == 0 ? src[0] : (z == 1 ? src[1] : src[2]);
+    return s0 + ((long long)x * g.M + j) * g.Kz + kz;
+  }
+  __device__ __forceinline__ C xform(int, int, int, int, C v) const { return v; }
+  __device__ __forceinline__ void store_z(int z, int x, int y, int kz, C v) const {
+    C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
+    d[((long long)x * g.M + y) * g.Kz + kz] = v;
+  }
 };
 
 // y pass of the product's r2c: keeps only the rows unpad reads
@@ -148,6 +178,12 @@ struct ConvYFwdOp {
     const int j = g.kept_row(y);
     if (j >= 0) dst[((long long)x * g.M + j) * g.Kz + kz] = v;
   }
+  static constexpr bool kPipe = true;
+  __device__ __forceinline__ const C* srcp(int, int x, int y, int kz) const {
+    return src + ((long long)x * g.M + y) * g.Kz + kz;
+  }
+  __device__ __forceinline__ C xform(int, int, int, int, C v) const { return v; }
+  __device__ __forceinline__ void store_z(int, int x, int y, int kz, C v) const { store(x, y, kz, v); }
 };
 
 // x pass of the product's r2c + unpad + output operator (+ optional inverse
@@ -193,6 +229,12 @@ struct ConvXFwdOp {
     target[idx] = r;
   }
   __device__ __forceinline__ void store(int j, int xx, int kz, C v) const { store_pre(j, xx, kz, v, prefetch(j, xx, kz)); }
+  static constexpr bool kPipe = true;
+  __device__ __forceinline__ const C* srcp(int, int j, int xx, int kz) const {
+    return src + ((long long)xx * g.M + j) * g.Kz + kz;
+  }
+  __device__ __forceinline__ C xform(int, int, int, int, C v) const { return v; }
+  __device__ __forceinline__ void store_z(int, int j, int xx, int kz, C v) const { store(j, xx, kz, v); }
 };
 
 // x pass of the c2r of one displacement / velocity component, with the
@@ -212,6 +254,7 @@ struct AssembleXInvOp {
   int n, Kz, d, s2x, s2y, s2z;
   T kfac, wA, unit;
   static constexpr bool kPrefetch = false;
+  static constexpr bool kPipe = false;
   __device__ __forceinline__ C load(int j, int i, int kz) const {
     const long long idx = ((long long)i * n + j) * Kz + kz;
     if (idx == 0) return mkc<T>(T(0), T(0));
@@ -253,6 +296,12 @@ struct PlainStridedOp {
   __device__ __forceinline__ void store(int slab, int e, int col, C v) const {
     p[(long long)slab * slab_str + (long long)e * e_str + col] = mkc<T>(v.x * scale, v.y * scale);
   }
+  static constexpr bool kPipe = true;
+  __device__ __forceinline__ const C* srcp(int, int slab, int e, int col) const {
+    return p + (long long)slab * slab_str + (long long)e * e_str + col;
+  }
+  __device__ __forceinline__ C xform(int, int, int, int, C v) const { return v; }
+  __device__ __forceinline__ void store_z(int, int slab, int e, int col, C v) const { store(slab, e, col, v); }
 };
 
 // plain z pass on the in-place padded layout: line = i*n + j, row of n+2 reals
