@@ -139,6 +139,25 @@ int mf_conv_convolve3(mf_conv* cv, const mf_operand* a, const mf_operand* b, con
 int mf_conv_convolve2_invlap(mf_conv* cv, const mf_operand* a, const mf_operand* b, mf_grid* out, int op,
                              double x);
 
+/* Orszag 3/2 convolve2 that allocates nothing -- no counterpart in the
+ * reference.  For callers that cannot allocate device memory: a simulation
+ * code embedding the generator whose memory pool already owns the device, or
+ * host code that must not incur the implicit synchronisation of
+ * cudaMalloc/cudaFree.  Inputs and output are caller-owned device arrays in
+ * the k-space layout of an n-grid (n x n x (n/2+1) complex of the given
+ * precision); the padded work buffers live in one static 48 MiB device array
+ * that the library holds on every device it is loaded on, which limits this
+ * call to n <= 128 (FP32) and n <= 96 (FP64); larger sizes return
+ * MF_ERR_SHAPE.  The first call on a device looks up that array's device
+ * address and should come before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race; the call returns when the
+ * result is complete (MF_ERR_TIMEOUT if a bounded wait ran out).  kind_a /
+ * kind_b are MF_OPND_* with directions dirs_a / dirs_b (4 ints each), op is
+ * MF_OP_* applied to out with factor x. */
+int mf_conv_convolve2_noalloc(void* stream, int n, double boxlen, int prec, const void* field_a, int kind_a,
+                              const int* dirs_a, const void* field_b, int kind_b, const int* dirs_b, void* out,
+                              int op, double x);
+
 #ifdef __cplusplus
 }
 #endif
