@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 METRIC = "3LPT particles/s at 512^3: FP32-bulk vs FP64 plain (1 GB300); p50/p99 IC latency"
 UNIT = "particles/s"
 
-WORKLOAD = dict(ngrid=512, boxlen=1000.0, zstart=24.0, lpt_order=3, lattice="bcc")
+WORKLOAD = dict(ngrid=512, boxlen=1000.0, zstart=24.0, lpt_order=3, lattice="bcc", plt=True)
 COSMO = dict(Omega_m=0.3099, Omega_b=0.0488, h=0.6774, sigma_8=0.8102, n_s=0.9667)
 
 
@@ -241,7 +241,8 @@ def run_mf(args):
     def make(prec):
         cfg = ic.ICConfig(ngrid=n, boxlen=WORKLOAD["boxlen"], zstart=WORKLOAD["zstart"],
                           lpt_order=WORKLOAD["lpt_order"], lattice=WORKLOAD["lattice"], precision=prec,
-                          lunit=WORKLOAD["boxlen"], vunit=WORKLOAD["boxlen"], pos64=(prec == "f64"), id64=True)
+                          lunit=WORKLOAD["boxlen"], vunit=WORKLOAD["boxlen"], pos64=(prec == "f64"), id64=True,
+                          plt=True)
         return ic.ICGenerator(ctx, cfg, sc)
 
     def timed(gen, steps, warmup, clocks=None, profile=False):
@@ -374,7 +375,7 @@ def run_mf(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": (f"3LPT BCC 2x{n}^3 particles, Orszag 3/2 (M={3 * n // 2}), L=1000 Mpc/h, z=24, "
                                     "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with FP64 order sum and q+Psi"),
-                       "plt": False, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"},
+                       "plt": True, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"},
             "latency_ms": {"p50": p50, "p99": p99},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -77,6 +77,7 @@ typedef struct {
   int out_kind;           /* MF_OUT_PARTICLES or MF_OUT_FIELDS              */
   int pos64;              /* output_plugin::has_64bit_reals                 */
   int id64;               /* output_plugin::has_64bit_ids                   */
+  int plt_ngrid;          /* PLT mesh size (lattice_gradient ngridself); 0: 64 */
 } mf_ic_params;
 
 /* Particle container (include/particle_container.hh:29-139): positions and
@@ -114,8 +115,14 @@ int mf_ic_stage_times(const mf_ic* ic, double* ms8);
  * before the growth factors of ic_generator.cc:550-563): which = 0 phi,
  * 1 phi2, 2 phi3, 3..5 A3x..z */
 int mf_ic_get_potential(mf_ic* ic, int which, mf_grid** out);
-/* Grid of the k-space white noise after normalisation (ic_generator.cc:341-346) */
+/* Grid of the k-space white noise after normalisation (ic_generator.cc:341-346);
+ * after mf_ic_run it holds the velocity order sum of the assembly stage */
 int mf_ic_get_noise(mf_ic* ic, mf_grid** out);
+
+/* PLT tables of lattice_gradient (include/particle_plt.hh:68-549) on an
+ * ng^3 mesh: real parts of D_r, D_theta, D_phi and the growth-rate
+ * correction, each ng*ng*(ng/2+1) doubles in k-space order */
+int mf_plt_tables(mf_ctx* ctx, int lattice, int ng, double* Dr, double* Dth, double* Dph, double* Dvf);
 
 #ifdef __cplusplus
 }

@@ -87,7 +87,7 @@ class mf_ic_params(C.Structure):
                 ("lattice", C.c_int), ("precision", C.c_int), ("convolver", C.c_int), ("fixing", C.c_int),
                 ("inversion", C.c_int), ("plt", C.c_int), ("cosmo", mf_cosmo_scalars),
                 ("tk_table", C.c_void_p), ("lunit", C.c_double), ("vunit", C.c_double), ("out_kind", C.c_int),
-                ("pos64", C.c_int), ("id64", C.c_int)]
+                ("pos64", C.c_int), ("id64", C.c_int), ("plt_ngrid", C.c_int)]
 
 
 class mf_particles(C.Structure):
@@ -113,6 +113,7 @@ SIGNATURES.update({
     "mf_ic_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "mf_ic_get_potential": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "mf_ic_get_noise": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "mf_plt_tables": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 })
 
 _lib = None

@@ -11,6 +11,7 @@
 #include "../../include/monofonic_gb300_ic.h"
 #include "mf_cosmo.h"
 #include "mf_eh.cuh"
+#include "mf_plt.h"
 #include "mf_runtime.h"
 
 namespace mf {
@@ -137,6 +138,8 @@ struct mf_ic {
   mf_grid* tmp[3] = {nullptr, nullptr, nullptr};  // real-space components of one sub-lattice
   void* phase = nullptr;  // exp(+2 pi i m / 2n), m in [0, 2n), grid precision
   double* qtab = nullptr; // lattice coordinates q[ishift][d][idx] * lunit
+  void* plt = nullptr;    // PLT tables Dr, Dth, Dph, Dvf in the grid precision
+  int plt_ng = 0;
   mf_conv* conv = nullptr;
   double* amp = nullptr;
   int nk2 = 0;
@@ -161,7 +164,7 @@ int check_params(const mf_ic_params* p) {
   if (p->out_kind != MF_OUT_PARTICLES && p->out_kind != MF_OUT_FIELDS) return MF_ERR_ARG;
   if (p->out_kind == MF_OUT_FIELDS && p->lattice != MF_LATTICE_SC) return MF_ERR_ARG;
   if (!(p->boxlen > 0)) return MF_ERR_ARG;
-  if (p->plt) return MF_ERR_ARG;  // PLT tables are built by mf_ic_create when supported
+  if (p->plt && p->plt_ngrid != 0 && !grid_size_supported(p->plt_ngrid)) return MF_ERR_SHAPE;
   return MF_OK;
 }
 
@@ -343,6 +346,19 @@ int run_impl(mf_ic* ic, mf_particles* out) {
         op.kfac = T(kfac);
         op.wA = T(wA);
         op.unit = T((vel ? p.vunit : p.lunit) / L);
+        op.plt = p.plt;
+        op.vel = vel ? 1 : 0;
+        if (p.plt) {
+          const size_t nkt = (size_t)ic->plt_ng * ic->plt_ng * (ic->plt_ng / 2 + 1);
+          const T* base = (const T*)ic->plt;
+          op.P.Dr = base;
+          op.P.Dth = base + nkt;
+          op.P.Dph = base + 2 * nkt;
+          op.P.Dvf = base + 3 * nkt;
+          op.P.ng = ic->plt_ng;
+          op.P.mapratio = T((double)ic->plt_ng / (double)n);
+          op.P.inv_mr_L = T(1.0 / ((double)ic->plt_ng / (double)n) / L);
+        }
         {
           LaunchScope ls(c, KK_FFT_COL);
           CK(Launch<T>::assemble_xinv(n, op, n, Kz, twN, s));
@@ -449,6 +465,7 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
     if (g) mf_grid_destroy(g);
   cudaFree(ic->phase);
   cudaFree(ic->qtab);
+  cudaFree(ic->plt);
   if (ic->conv) mf_conv_destroy(ic->conv);
   cudaFree(ic->amp);
   cudaFree(ic->dpos);
@@ -515,6 +532,23 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     e2 = cudaMalloc(&ic->qtab, q.size() * sizeof(double));
     if (e2 == cudaSuccess) e2 = cudaMemcpy(ic->qtab, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
     if (e2 != cudaSuccess) return fail(cuda_err(c, e2, "mf_ic_create: lattice table"));
+  }
+  if (p->plt) {
+    PLTTables t;
+    ic->plt_ng = p->plt_ngrid ? p->plt_ngrid : 64;
+    if ((rc = plt_build_tables(c, p->lattice, ic->plt_ng, &t))) return fail(rc);
+    const size_t nkt = t.Dr.size();
+    const size_t es = (p->precision == MF_PREC_F32) ? sizeof(float) : sizeof(double);
+    std::vector<unsigned char> h(4 * nkt * es);
+    const std::vector<double>* src[4] = {&t.Dr, &t.Dth, &t.Dph, &t.Dvf};
+    for (int a = 0; a < 4; ++a)
+      for (size_t q = 0; q < nkt; ++q) {
+        if (es == sizeof(float)) reinterpret_cast<float*>(h.data())[a * nkt + q] = (float)(*src[a])[q];
+        else reinterpret_cast<double*>(h.data())[a * nkt + q] = (*src[a])[q];
+      }
+    cudaError_t e3 = cudaMalloc(&ic->plt, h.size());
+    if (e3 == cudaSuccess) e3 = cudaMemcpy(ic->plt, h.data(), h.size(), cudaMemcpyHostToDevice);
+    if (e3 != cudaSuccess) return fail(cuda_err(c, e3, "mf_ic_create: PLT tables"));
   }
   if (p->lpt_order > 1)
     if ((rc = mf_conv_create(c, n, p->boxlen, p->precision, p->convolver, &ic->conv))) return fail(rc);

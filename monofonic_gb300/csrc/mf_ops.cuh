@@ -11,6 +11,7 @@
 #pragma once
 
 #include "mf_fft.cuh"
+#include "mf_plt_dev.cuh"
 
 namespace mf {
 
@@ -253,20 +254,37 @@ struct AssembleXInvOp {
   const C* phase;   // 2n entries, nullptr for the unshifted lattice
   int n, Kz, d, s2x, s2y, s2z;
   T kfac, wA, unit;
+  int plt;          // PLT corrected gradient (lattice_gradient, particle_plt.hh:551-573)
+  int vel;          // velocities: times the PLT growth-rate correction vfac_corr (:575-585)
+  PLTDev<T> P;
   static constexpr bool kPrefetch = false;
   static constexpr bool kPipe = false;
   __device__ __forceinline__ C load(int j, int i, int kz) const {
     const long long idx = ((long long)i * n + j) * Kz + kz;
     if (idx == 0) return mkc<T>(T(0), T(0));
-    const C P = phitot[idx];
-    const T gd = gradk<T>(sel3(d, i, j, kz), n, kfac);
-    T rr = -gd * P.y, ri = gd * P.x;
+    const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
+    T gd, gp, gpp, vc = T(1);
+    if (plt) {
+      T g[3];
+      plt_gradient<T>(P, i, j, kz, g, vel ? &vc : nullptr);
+      gd = (d == 0) ? g[0] : ((d == 1) ? g[1] : g[2]);
+      gp = (dp == 0) ? g[0] : ((dp == 1) ? g[1] : g[2]);
+      gpp = (dpp == 0) ? g[0] : ((dpp == 1) ? g[1] : g[2]);
+    } else {
+      gd = gradk<T>(sel3(d, i, j, kz), n, kfac);
+      gp = gradk<T>(sel3(dp, i, j, kz), n, kfac);
+      gpp = gradk<T>(sel3(dpp, i, j, kz), n, kfac);
+    }
+    const C P1 = phitot[idx];
+    T rr = -gd * P1.y, ri = gd * P1.x;
     if (A3p) {
-      const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
-      const T gp = gradk<T>(sel3(dp, i, j, kz), n, kfac), gpp = gradk<T>(sel3(dpp, i, j, kz), n, kfac);
       const C X1 = A3pp[idx], X2 = A3p[idx];
       rr += wA * (-(gp * X1.y) + gpp * X2.y);
       ri += wA * (gp * X1.x - gpp * X2.x);
+    }
+    if (plt && vel) {
+      rr *= vc;
+      ri *= vc;
     }
     rr *= unit;
     ri *= unit;

@@ -83,6 +83,7 @@ class ICConfig:
     out_kind: str = "particles"
     pos64: bool = True
     id64: bool = True
+    plt_ngrid: int = 0
 
     def to_c(self, scalars, tk_table=None):
         p = L.mf_ic_params()
@@ -103,6 +104,7 @@ class ICConfig:
         p.out_kind = L.MF_OUT_PARTICLES if self.out_kind == "particles" else L.MF_OUT_FIELDS
         p.pos64 = int(self.pos64)
         p.id64 = int(self.id64)
+        p.plt_ngrid = int(self.plt_ngrid)
         return p
 
 
@@ -213,6 +215,14 @@ class PinnedBuffer:
             self.close()
         except Exception:
             pass
+
+
+def plt_tables(ctx: Context, lattice: str, ng: int = 64):
+    """PLT tables (D_r, D_theta, D_phi, vfac correction), each (ng, ng, ng/2+1)."""
+    shape = (ng, ng, ng // 2 + 1)
+    out = [np.empty(shape) for _ in range(4)]
+    _check(ctx.ptr, lib().mf_plt_tables(ctx.ptr, LATTICES[lattice], int(ng), *[a.ctypes.data for a in out]))
+    return out
 
 
 def device_footprint(cfg: ICConfig, scalars) -> int:

@@ -743,3 +743,230 @@ def power_spectrum(F, L):
         bP = np.where(bc > 0, bP / bc * volfac * fftfac, 0)
         beP = np.where(bc > 0, np.sqrt(beP / bc - bP * bP) / np.sqrt(bc) * volfac * fftfac, 0)
     return bk, bP, beP, bc.astype(np.int64)
+
+
+# ----------------------------------------------------------------------------
+# PLT corrections (include/particle_plt.hh:50-587)
+# ----------------------------------------------------------------------------
+def _plt_lattice(lattice):
+    """Bravais / reciprocal / inverse-reciprocal matrices, FBZ normals and
+    charge factor (particle_plt.hh:76-164); RSC falls back to SC (:166-172)."""
+    pi, twopi, fourpi = math.pi, 2 * math.pi, 4 * math.pi
+    if lattice == 1:
+        B = np.array([[1, 0, 0.5], [0, 1, 0.5], [0, 0, 0.5]])
+        R = np.array([[twopi, 0, 0], [0, twopi, 0], [-twopi, -twopi, fourpi]])
+        IR = np.array([[2, 0, 0], [0, 2, 0], [1, 1, 1]])
+        nrm = [(0, pi, pi), (0, -pi, pi), (0, pi, -pi), (0, -pi, -pi), (pi, 0, pi), (-pi, 0, pi),
+               (pi, 0, -pi), (-pi, 0, -pi), (pi, pi, 0), (-pi, pi, 0), (pi, -pi, 0), (-pi, -pi, 0)]
+        cf = 2
+    elif lattice == 2:
+        B = np.array([[0, 0.5, 0], [0.5, 0, 1], [0.5, 0.5, 0]])
+        R = np.array([[-fourpi, fourpi, twopi], [0, 0, twopi], [fourpi, 0, -twopi]])
+        IR = np.array([[0, 1, 1], [1, 0, 1], [0, 2, 0]])
+        nrm = [(twopi, 0, 0), (-twopi, 0, 0), (0, twopi, 0), (0, -twopi, 0), (0, 0, twopi), (0, 0, -twopi),
+               (pi, pi, pi), (pi, pi, -pi), (pi, -pi, pi), (pi, -pi, -pi), (-pi, pi, pi), (-pi, pi, -pi),
+               (-pi, -pi, pi), (-pi, -pi, -pi)]
+        cf = 4
+    else:
+        B = np.eye(3)
+        R = np.eye(3) * twopi
+        IR = np.eye(3, dtype=int) * 2
+        nrm = [(pi, 0, 0), (-pi, 0, 0), (0, pi, 0), (0, -pi, 0), (0, 0, pi), (0, 0, -pi)]
+        cf = 1
+    return B.astype(float), R.astype(float), IR.astype(int), np.array(nrm, dtype=float), cf
+
+
+def plt_tables(lattice, ng):
+    """lattice_gradient::init_D (particle_plt.hh:68-515), vectorised; returns
+    the real tables (D_r, D_theta, D_phi, D_vfac) on the (ng, ng, ng/2+1)
+    k-space mesh.  Map insertions follow the sequential loop order (first
+    insertion of a key wins)."""
+    B, R, IR, normals, cf = _plt_lattice(lattice)
+    nl = ng
+    dx = 1.0 / nl
+    eta = 4.0
+    alpha = 1.0 / math.sqrt(2) / eta
+    a2, a3 = alpha * alpha, alpha ** 3
+    charge = 1.0 / nl ** 3 / cf
+    fft_norm = 1.0 / nl ** 3.0
+    idx = np.arange(nl)
+    X = np.stack(np.meshgrid(idx, idx, idx, indexing="ij"), -1).reshape(-1, 3) * dx
+    ar = np.fmod(2.0 + X @ B.T, 1.0)
+    M = np.zeros((ar.shape[0], 3, 3))
+    rng = range(-3, 4)
+    for ix in rng:
+        for iy in rng:
+            for iz in rng:
+                d = ar - B @ np.array([ix, iy, iz], dtype=float)
+                r = np.sqrt(np.sum(d * d, axis=1))
+                ok = r >= 1e-14
+                rs = np.where(ok, r, 1.0)
+                r2, r3, r5 = rs * rs, rs ** 3, rs ** 5
+                K1 = -a3 / math.pi ** 1.5 * np.exp(-a2 * r2) / r2
+                from scipy.special import erfc
+                K2 = (erfc(alpha * rs) + 2.0 * alpha / math.sqrt(math.pi) * np.exp(-a2 * r2) * rs) / (4 * math.pi)
+                dd = d[:, :, None] * d[:, None, :]
+                add = dd * K1[:, None, None] + (np.eye(3)[None] / r3[:, None, None] - 3.0 * dd / r5[:, None, None]) * K2[:, None, None]
+                M += np.where(ok[:, None, None], add, 0.0)
+    for ix in rng:
+        for iy in rng:
+            for iz in rng:
+                if abs(ix) + abs(iy) + abs(iz) == 0:
+                    continue
+                ak = R @ (np.array([ix, iy, iz], dtype=float) / nl)
+                km2 = ak @ ak
+                term = np.exp(-km2 / (4 * a2)) * np.cos(ar @ ak) / km2 * fft_norm
+                M += np.outer(ak, ak)[None] * term[:, None, None]
+    D6 = [M[:, a, b].reshape(nl, nl, nl) * charge for a, b in ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))]
+    for a, v in enumerate((1.0 / 3, 0.0, 0.0, 1.0 / 3, 0.0, 1.0 / 3)):
+        D6[a][0, 0, 0] = v
+    Dk = [np.fft.rfftn(f).real for f in D6]  # unitary r2c times nl^1.5 = plain DFT
+    nk = nl // 2 + 1
+    kc = (np.arange(nl) - (np.arange(nl) > nl // 2) * nl) * 2 * math.pi
+    KX, KY, KZ = np.meshgrid(kc, kc, kc[:nk], indexing="ij")
+    kv = np.stack([KX, KY, KZ], -1).reshape(-1, 3)
+    Dm = np.empty((kv.shape[0], 3, 3))
+    for (a, b), f in zip(((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)), Dk):
+        Dm[:, a, b] = Dm[:, b, a] = f.reshape(-1)
+    ev, V = np.linalg.eigh(Dm)  # ascending
+    e3 = V[:, :, 2] / (2 * math.pi * ng)
+    T = np.stack([Dk[0].reshape(-1), Dk[1].reshape(-1), Dk[2].reshape(-1), Dk[3].reshape(-1),
+                  Dk[4].reshape(-1), Dk[5].reshape(-1)], 1)
+    a_vec = (kv / (2 * math.pi * ng)) @ R.T
+    shifts = [(l1, l2, l3, s) for l1 in (-1, 0, 1) for l2 in (-1, 0, 1) for l3 in (-1, 0, 1) for s in (-1.0, 1.0)]
+    keys_all, q_all, valid_all = [], [], []
+    for (l1, l2, l3, sg) in shifts:
+        vk = sg * a_vec + R @ np.array([l1, l2, l3], dtype=float)
+        ok = np.all(vk @ normals.T <= 1.0001 * np.sum(normals * normals, axis=1)[None], axis=1)
+        key = np.round(vk * ng / (2 * math.pi)).astype(np.int64)
+        keys_all.append(key)
+        valid_all.append(ok)
+    keys_all = np.stack(keys_all, 1)  # (nq, nshift, 3)
+    valid_all = np.stack(valid_all, 1)
+    anyv = valid_all.any(axis=1)
+    T[anyv] = np.stack([ev[anyv, 2], ev[anyv, 1], ev[anyv, 0], e3[anyv, 0], e3[anyv, 1], e3[anyv, 2]], 1)
+    off, K = 8 * ng, 16 * ng
+    enc = lambda k: ((k[..., 0] + off) * K + (k[..., 1] + off)) * K + (k[..., 2] + off)
+    flat_keys = enc(keys_all).reshape(-1)
+    flat_q = np.repeat(np.arange(kv.shape[0]), len(shifts))
+    sel = valid_all.reshape(-1)
+    fk, fq = flat_keys[sel], flat_q[sel]
+    ukeys, first = np.unique(fk, return_index=True)
+    uq = fq[first]
+
+    def lookup(k):
+        e = enc(k)
+        pos = np.clip(np.searchsorted(ukeys, e), 0, len(ukeys) - 1)
+        found = ukeys[pos] == e
+        return np.where(found, uq[pos], -1)
+
+    ii = np.arange(nl) - (np.arange(nl) > nl // 2) * nl
+    kk = np.arange(nk) - (np.arange(nk) > nl // 2) * nl
+    I, J, Kq = np.meshgrid(ii, ii, kk, indexing="ij")
+    sgn = np.stack([I, J, Kq], -1).reshape(-1, 3)
+    ui, uj, uk = np.meshgrid(np.arange(nl), np.arange(nl), np.arange(nk), indexing="ij")
+    uidx = np.stack([ui, uj, uk], -1).reshape(-1, 3)
+    isin = np.all((uidx @ IR.T) % 2 == 0, axis=1)
+    kvv = sgn.astype(float)
+
+    def align(v):
+        return v * np.where(np.sum(v * kvv, axis=1) < 0, -1.0, 1.0)[:, None]
+
+    l = np.zeros((kv.shape[0], 3))
+    v = np.zeros((kv.shape[0], 3))
+    cnt = np.zeros(kv.shape[0])
+    for o in ((-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
+        q = lookup(sgn + np.array(o))
+        f = (q >= 0) & ~isin
+        qq = np.where(q >= 0, q, 0)
+        l += np.where(f[:, None], T[qq][:, 0:3], 0.0)
+        v += np.where(f[:, None], align(T[qq][:, 3:6]), 0.0)
+        cnt += f
+    with np.errstate(invalid="ignore", divide="ignore"):
+        l = np.where(~isin[:, None], l / cnt[:, None], l)
+        v = np.where(~isin[:, None], v / cnt[:, None], v)
+    q = lookup(sgn)
+    f = isin & (q >= 0)
+    qq = np.where(q >= 0, q, 0)
+    l = np.where(f[:, None], T[qq][:, 0:3], np.where(isin[:, None], 0.0, l))
+    v = np.where(f[:, None], align(T[qq][:, 3:6]), np.where(isin[:, None], 0.0, v))
+    mu1 = l[:, 0]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        e1 = v / np.linalg.norm(v, axis=1)[:, None]
+    kr = np.linalg.norm(kv, axis=1)
+    kphi = np.where(kr > 0, np.arctan2(kv[:, 1], kv[:, 0]), 0.0)
+    kth = np.where(kr > 0, np.arccos(np.where(kr > 0, kv[:, 2] / np.where(kr > 0, kr, 1), 1.0)), 0.0)
+    st, ct, sp, cp = np.sin(kth), np.cos(kth), np.sin(kphi), np.cos(kphi)
+    e_r = np.stack([st * cp, st * sp, ct], 1)
+    e_t = np.stack([ct * cp, ct * sp, -st], 1)
+    e_p = np.stack([-sp, cp, 0 * sp], 1)
+    ren = np.sum(e1 * e_r, 1)
+    ren = np.where(ren < 0.01, 1.0, ren)
+    Dr = np.ones(kv.shape[0])
+    Dth = np.sum(e1 * e_t, 1) / ren
+    Dph = np.sum(e1 * e_p, 1) / ren
+    with np.errstate(invalid="ignore", divide="ignore"):
+        Dvf = 1.0 / (0.25 * (np.sqrt(1.0 + 24 * mu1) - 1.0))
+    Dvf[0], Dr[0], Dth[0], Dph[0] = 1.0, 1.0, 0.0, 0.0
+    shp = (nl, nl, nk)
+    return Dr.reshape(shp), Dth.reshape(shp), Dph.reshape(shp), Dvf.reshape(shp)
+
+
+def _cic_kspace(tab, x, y, z):
+    """get_cic_kspace (grid_fft.hh:347-373) of a real table, vectorised."""
+    ng = tab.shape[0]
+    nk = tab.shape[2]
+    ix, iy, iz = np.floor(x).astype(int), np.floor(y).astype(int), np.floor(z).astype(int)
+    dx, dy, dz = x - ix, y - iy, z - iz
+    tx, ty, tz = 1 - dx, 1 - dy, 1 - dz
+    ix1, iy1, iz1 = (ix + 1) % ng, (iy + 1) % ng, np.minimum(iz + 1, nk - 1)
+    return (tab[ix, iy, iz] * tx * ty * tz + tab[ix, iy, iz1] * tx * ty * dz + tab[ix, iy1, iz] * tx * dy * tz
+            + tab[ix, iy1, iz1] * tx * dy * dz + tab[ix1, iy, iz] * dx * ty * tz + tab[ix1, iy, iz1] * dx * ty * dz
+            + tab[ix1, iy1, iz] * dx * dy * tz + tab[ix1, iy1, iz1] * dx * dy * dz)
+
+
+def plt_gradient(tables, n, L):
+    """lattice_gradient::gradient / vfac_corr (particle_plt.hh:551-585) on
+    the n-grid half spectrum: returns ([g_x, g_y, g_z], vfac_corr) with the
+    gradient i*g_d."""
+    Dr_t, Dth_t, Dph_t, Dvf_t = tables
+    ng = Dr_t.shape[0]
+    mr = ng / n
+    i = np.arange(n) * mr
+    kz_ = np.arange(n // 2 + 1) * mr
+    X, Y, Z = np.meshgrid(i, i, kz_, indexing="ij")
+    kcomp = lambda a: (a - (a > ng // 2) * ng) * 2 * math.pi
+    kx, ky, kz = kcomp(X), kcomp(Y), kcomp(Z)
+    kr = np.sqrt(kx * kx + ky * ky + kz * kz)
+    kmod = kr / mr / L
+    D_r, D_t, D_p = _cic_kspace(Dr_t, X, Y, Z), _cic_kspace(Dth_t, X, Y, Z), _cic_kspace(Dph_t, X, Y, Z)
+    kphi = np.where(kr > 0, np.arctan2(ky, kx), 0.0)
+    kth = np.where(kr > 0, np.arccos(np.where(kr > 0, kz / np.where(kr > 0, kr, 1), 1.0)), 0.0)
+    st, ct, sp, cp = np.sin(kth), np.cos(kth), np.sin(kphi), np.cos(kphi)
+    g = [kmod * (D_r * st * cp + D_t * ct * cp - D_p * sp),
+         kmod * (D_r * st * sp + D_t * ct * sp + D_p * cp),
+         kmod * (D_r * ct - D_t * st)]
+    return g, _cic_kspace(Dvf_t, X, Y, Z)
+
+
+def displacement_k_plt(f: LPTFields, L, d, order, tables, unit=1.0, vel=False, vfac=0.0):
+    """ic_generator.cc:829-931 with the PLT lattice_gradient in place of
+    op::fourier_gradient (ENABLE_PLT, ic_generator.cc:366-370)."""
+    n = f.phi.shape[0]
+    g, vc = plt_gradient(tables, n, L)
+    dp, dpp = (d + 1) % 3, (d + 2) % 3
+    w = [1.0, 1.0, 1.0] if not vel else [vfac, 2 * vfac, 3 * vfac]
+    tot = w[0] * f.phi
+    if order > 1:
+        tot = tot + w[1] * f.phi2
+    if order > 2:
+        tot = tot + w[2] * f.phi3
+    t = (1j * g[d]) * tot
+    if order > 2:
+        a = (1j * g[dp]) * f.A3[dpp] - (1j * g[dpp]) * f.A3[dp]
+        t = t + (3 * vfac if vel else 1.0) * a
+    if vel:
+        t = t * vc
+    t = t * (unit / L)
+    t[0, 0, 0] = 0
+    return t
