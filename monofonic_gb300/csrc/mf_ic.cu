@@ -336,13 +336,15 @@ int run_impl(mf_ic* ic, mf_particles* out) {
         op.A3p = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 1) % 3]->d : nullptr;
         op.A3pp = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 2) % 3]->d : nullptr;
         op.dst = tk;
-        op.phase = ish > 0 ? (const cplx<T>*)ic->phase : nullptr;
+        op.phase = (const cplx<T>*)ic->phase;
         op.n = n;
         op.Kz = Kz;
         op.d = d;
-        op.s2x = (int)lround(2 * kShifts[p.lattice][ish][0]);
-        op.s2y = (int)lround(2 * kShifts[p.lattice][ish][1]);
-        op.s2z = (int)lround(2 * kShifts[p.lattice][ish][2]);
+        // relative shifts of set_positions / set_velocities (particle_generator.hh:505-522)
+        op.nstep = ish;
+        for (int st = 1; st <= ish; ++st)
+          for (int q = 0; q < 3; ++q)
+            op.s2[st - 1][q] = (int)lround(2 * (kShifts[p.lattice][st][q] - kShifts[p.lattice][st - 1][q]));
         op.kfac = T(kfac);
         op.wA = T(wA);
         op.unit = T((vel ? p.vunit : p.lunit) / L);

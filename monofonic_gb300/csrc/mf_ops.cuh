@@ -251,15 +251,21 @@ struct AssembleXInvOp {
   const C* A3p;     // A3[d'] (nullptr below 3LPT)
   const C* A3pp;    // A3[d'']
   C* dst;
-  const C* phase;   // 2n entries, nullptr for the unshifted lattice
-  int n, Kz, d, s2x, s2y, s2z;
+  const C* phase;   // 2n entries exp(+2 pi i m / 2n)
+  int n, Kz, d;
+  // sub-lattice: nstep relative shifts (shift_field calls of
+  // particle_generator.hh:505-522), each 2*(s_ish - s_{ish-1}) in {-1,0,1}
+  int nstep;
+  int s2[7][3];
   T kfac, wA, unit;
   int plt;          // PLT corrected gradient (lattice_gradient, particle_plt.hh:551-573)
   int vel;          // velocities: times the PLT growth-rate correction vfac_corr (:575-585)
   PLTDev<T> P;
   static constexpr bool kPrefetch = false;
   static constexpr bool kPipe = false;
-  __device__ __forceinline__ C load(int j, int i, int kz) const {
+
+  // k-space combination at (i, j, kz) before any sub-lattice phase
+  __device__ __forceinline__ C assemble(int i, int j, int kz) const {
     const long long idx = ((long long)i * n + j) * Kz + kz;
     if (idx == 0) return mkc<T>(T(0), T(0));
     const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
@@ -286,15 +292,35 @@ struct AssembleXInvOp {
       rr *= vc;
       ri *= vc;
     }
-    rr *= unit;
-    ri *= unit;
-    if (phase) {
-      const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
-      int m = (s2x * ii + s2y * jj + s2z * kz) % (2 * n);
-      if (m < 0) m += 2 * n;
-      return cmul(mkc<T>(rr, ri), phase[m]);
+    return mkc<T>(rr * unit, ri * unit);
+  }
+  // phase of relative shift step s at (i, j, kz): exp(i dS.k dx), k = get_k
+  // (Nyquist index positive), dS = s2/2
+  __device__ __forceinline__ C step_phase(int s, int i, int j, int kz) const {
+    const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
+    int m = (s2[s][0] * ii + s2[s][1] * jj + s2[s][2] * kz) % (2 * n);
+    if (m < 0) m += 2 * n;
+    return phase[m];
+  }
+  __device__ __forceinline__ C load(int j, int i, int kz) const {
+    C v = assemble(i, j, kz);
+    if (nstep == 0) return v;
+    if (kz == 0 || kz == (n >> 1)) {
+      // the reference re-projects onto real fields (r2c of the c2r) before
+      // every shift; on the kz = 0 and kz = n/2 planes that projection pairs
+      // k with -k: H(X)(k) = (X(k) + conj X(-k)) / 2
+      const int im = (n - i) % n, jm = (n - j) % n;
+      C vm = assemble(im, jm, kz);
+      for (int s = 0; s < nstep; ++s) {
+        const C hk = mkc<T>(T(0.5) * (v.x + vm.x), T(0.5) * (v.y - vm.y));
+        const C hm = mkc<T>(T(0.5) * (vm.x + v.x), T(0.5) * (vm.y - v.y));
+        v = cmul(hk, step_phase(s, i, j, kz));
+        vm = cmul(hm, step_phase(s, im, jm, kz));
+      }
+      return v;
     }
-    return mkc<T>(rr, ri);
+    for (int s = 0; s < nstep; ++s) v = cmul(v, step_phase(s, i, j, kz));
+    return v;
   }
   __device__ __forceinline__ void store(int j, int i, int kz, C v) const { dst[((long long)i * n + j) * Kz + kz] = v; }
 };
