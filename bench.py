@@ -56,6 +56,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-items", type=int, default=96)
+    ap.add_argument("--batch-streams", type=int, default=8)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-seconds-fp64", type=float, default=6.0)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-workers", type=int, default=4)
     return ap.parse_args()
 
 
@@ -136,6 +144,22 @@ def algorithmic_bytes(kind: str, n: int, prec_bytes: int) -> float:
     return float("nan")
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch from
+# ncu captures of smaller cases, per unit of work (M^2 (N/2+1) line-modes of
+# the padded work buffer), so that it scales to the bench's grid size
+TRAFFIC_PER_UNIT = {
+    ("conv_z", 4): (408.3e6 / (384 * 384 * 129), "ncu --set full, k_zconv_tma N=256 (M=384) FP32, one launch"),
+}
+
+
+def traffic_per_launch(kind: str, n: int, prec_bytes: int):
+    t = TRAFFIC_PER_UNIT.get((kind, prec_bytes))
+    if t is None:
+        return None, None
+    M, Kz = 3 * n // 2, n // 2 + 1
+    return t[0] * M * M * Kz, t[1] + f", scaled to N={n} by M^2 (N/2+1)"
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -196,6 +220,121 @@ def run_reference(args):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+# ---------------------------------------------------------------------------
+# batched realizations and the IC server
+# ---------------------------------------------------------------------------
+BATCH_SIZES = (64, 96, 128, 192, 256)
+SERVE_SIZES = (64, 128, 192, 256, 384)
+
+
+def _draw_cosmology(rng):
+    from monofonic_gb300 import ic
+    return ic.Cosmology(Omega_m=float(rng.uniform(0.25, 0.35)), Omega_b=COSMO["Omega_b"], h=COSMO["h"],
+                        sigma_8=float(rng.uniform(0.7, 0.9)), n_s=float(rng.uniform(0.92, 1.0)))
+
+
+def _draw_request(rng, sizes, prec):
+    from monofonic_gb300.serve import Request
+    n = int(rng.choice(sizes))
+    return Request(ngrid=n, boxlen=2.0 * n, zstart=WORKLOAD["zstart"], lpt_order=int(rng.choice([2, 3])),
+                   lattice="sc", precision=prec, cosmology=_draw_cosmology(rng), seed=int(rng.integers(1, 2 ** 62)))
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))]
+
+
+def run_batch(args, device):
+    """Ragged batch of realizations recorded into one CUDA graph: N drawn from
+    {64,96,128,192,256}, L = 2N Mpc/h, 2LPT or 3LPT (p = 1/2), per-item seed
+    and cosmology (Omega_m U(.25,.35), sigma8 U(.7,.9), n_s U(.92,1)), FP32.
+    Each timed step draws new seeds and cosmologies (host cosmology on all
+    threads, timed separately) and replays the graph."""
+    import numpy as np
+    from monofonic_gb300.serve import Batch
+    rng = np.random.default_rng(2024)
+    reqs = [_draw_request(rng, BATCH_SIZES, "f32") for _ in range(args.batch_items)]
+    t0 = time.perf_counter()
+    b = Batch(reqs, nstreams=args.batch_streams, device=device)
+    t_create = time.perf_counter() - t0
+    info = b.info()
+    for _ in range(max(3, args.warmup)):
+        b.run()
+    dev_ms, host_ms = [], []
+    for _ in range(args.steps):
+        cos = [_draw_cosmology(rng) for _ in reqs]
+        seeds = [int(rng.integers(1, 2 ** 62)) for _ in reqs]
+        h0 = time.perf_counter()
+        b.set_items(0, cos, seeds)
+        host_ms.append((time.perf_counter() - h0) * 1e3)
+        dev_ms.append(b.run())
+    b.close()
+    npart = sum(r.npart for r in reqs)
+    ms = statistics.median(dev_ms)
+    return {"workload": (f"{len(reqs)} realizations, N in {{64,96,128,192,256}}, L=2N Mpc/h, 2LPT/3LPT p=0.5, "
+                         "SC, per-item seed and cosmology, FP32-bulk, noise generated on the device"),
+            "sizes": {str(n): sum(r.ngrid == n for r in reqs) for n in BATCH_SIZES},
+            "lpt3": sum(r.lpt_order == 3 for r in reqs), "particles": npart,
+            "streams": args.batch_streams, "graph_launches_per_batch": 1,
+            "graph_nodes": info["graph_nodes"], "kernels_per_batch": info["kernels"],
+            "device_GB": round(info["device_bytes"] / 1e9, 2), "create_s": round(t_create, 2),
+            "ms_per_batch": ms, "ms_per_batch_max": max(dev_ms),
+            "realizations_per_s": len(reqs) / (ms / 1e3), "particles_per_s": npart / (ms / 1e3),
+            "host_cosmology_ms": statistics.median(host_ms)}
+
+
+def run_serve(args, device, prec, seconds):
+    """Poisson stream of IC requests (rate args.serve_rate /s) for `seconds`:
+    N from {64,128,192,256,384}, L = 2N, 2LPT/3LPT p = 1/2, random seed and
+    cosmology; admission by device footprint; particles streamed to a counting
+    output callback in page-locked chunks.  The pool is warmed with one
+    request of every shape first."""
+    import numpy as np
+    from monofonic_gb300.serve import Server, Request
+    rng = np.random.default_rng(7 if prec == "f32" else 8)
+    srv = Server(nworkers=args.serve_workers, output="count", device=device)
+    for n in SERVE_SIZES:
+        for o in (2, 3):
+            srv.submit(Request(ngrid=n, boxlen=2.0 * n, zstart=WORKLOAD["zstart"], lpt_order=o, precision=prec))
+    srv.drain(600.0)
+    nwarm = srv.stats()["submitted"]
+    ids, npart = [], 0
+    start = time.perf_counter()
+    t_next = start
+    while t_next - start < seconds:
+        dt = t_next - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        r = _draw_request(rng, SERVE_SIZES, prec)
+        ids.append(srv.submit(r))
+        npart += r.npart
+        t_next += float(rng.exponential(1.0 / args.serve_rate))
+    drained = True
+    try:
+        srv.drain(max(120.0, 4 * seconds))
+    except Exception:
+        drained = False
+    res = [srv.wait(i, 0.0) for i in ids] if drained else []
+    st = srv.stats()
+    srv.close()
+    if not res:
+        return {"precision": prec, "requests": len(ids), "drained": False, "stats": st}
+    lat = [(r["t_done"] - r["t_submit"]) * 1e3 for r in res]
+    lat_gpu = [(r["t_gpu_done"] - r["t_submit"]) * 1e3 for r in res]
+    wait = [(r["t_admit"] - r["t_submit"]) * 1e3 for r in res]
+    span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+    ok = sum(r["status"] == 0 for r in res)
+    return {"precision": prec, "arrival_rate_per_s": args.serve_rate, "window_s": seconds, "requests": len(ids),
+            "completed": ok, "warmup_requests": nwarm, "workers": args.serve_workers,
+            "latency_ms": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99), "max": max(lat)},
+            "latency_to_device_done_ms": {"p50": _pct(lat_gpu, 0.5), "p99": _pct(lat_gpu, 0.99)},
+            "queue_wait_ms": {"p50": _pct(wait, 0.5), "p99": _pct(wait, 0.99)},
+            "particles_per_s": npart / span, "requests_per_s": len(ids) / span,
+            "gpu_ms_mean": statistics.mean(r["gpu_ms"] for r in res),
+            "peak_device_GB": round(st["peak_bytes"] / 1e9, 2), "pooled_pipelines": st["pooled_pipelines"]}
 
 
 # ---------------------------------------------------------------------------
@@ -366,6 +505,15 @@ def run_mf(args):
         except Exception as ex:  # the baseline must not break the GPU line
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch(args, local)
+    serving = None
+    if not args.no_serve:
+        serving = {"f32": run_serve(args, local, "f32", args.serve_seconds)}
+        if not args.no_fp64:
+            serving["f64"] = run_serve(args, local, "f64", args.serve_seconds_fp64)
+
     if rank == 0:
         p50 = lat[len(lat) // 2]
         p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
@@ -379,14 +527,18 @@ def run_mf(args):
             "latency_ms": {"p50": p50, "p99": p99},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "peak_source": "measured" if peaks else "fallback"},
+                         "frac": achieved / peak, "traffic": traffic_per_launch(dom, n, 4)[0],
+                         "traffic_source": traffic_per_launch(dom, n, 4)[1],
+                         "algorithmic_bytes_per_launch": bpl,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"},
             "kernels": kinds,
             "stages_ms": stages32,
             "e2e": e2e,
             "fp64_plain": fp64,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "batch": batch,
+            "serving": serving,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -83,6 +83,9 @@ int mf_probe_fma_rate(mf_ctx* ctx, int prec, double* tflops);
 /* page-locked host memory for streaming transfers (no reference counterpart) */
 int mf_host_alloc(size_t bytes, void** out);
 int mf_host_free(void* p);
+/* synchronous copy of device memory (e.g. particles of mf_ic_particles) to
+ * host memory (no reference counterpart) */
+int mf_copy_to_host(void* host, const void* device, size_t bytes);
 /* 1 if grid size n is supported by the compiled kernels */
 int mf_grid_size_supported(int n);
 

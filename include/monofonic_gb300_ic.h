@@ -50,10 +50,17 @@ int mf_eh_transfer(const mf_cosmo_params* p, const double* k, double* out, size_
 
 /* ---- white noise: RNG plugin (include/random_plugin.hh:26-39) ----------- */
 /* i.i.d. N(0,1) float64 on an n^3 grid, cell (i*n+j)*n+k; Philox4x32-10 block
- * p = cell/2 at counter (p_lo, p_hi, 0, 0), key (seed_lo, seed_hi), two
- * 53-bit uniforms through Box-Muller (cos -> even cell, sin -> odd cell).
+ * p = cell/2 at counter (p_lo, p_hi, 0, 0), key (seed_lo, seed_hi); the two
+ * 53-bit integers b1, b2 of the block give u1 = (b1+1/2) 2^-53 and the angle
+ * t = 2 pi (b2+1/2) 2^-53, and Box-Muller gives r cos t (even cell) and
+ * r sin t (odd cell), r = sqrt(-2 ln u1).  ln, sin and cos are the library's
+ * own (IEEE basic operations only), so the host and the device generator
+ * (mf_grid_fill_white_noise, mf_ic_set_noise_seed) give the same bits.
  * Host, multithreaded (nthreads <= 0: all hardware threads). */
 int mf_white_noise_host(int n, uint64_t seed, double* out, int nthreads);
+/* RNG_plugin::Fill_Grid on the device: the same field written into a
+ * real-space grid (values rounded to the grid precision); n even */
+int mf_grid_fill_white_noise(mf_grid* g, uint64_t seed);
 
 /* ---- LPT pipeline (src/ic_generator.cc:90-948) -------------------------- */
 enum { MF_OUT_PARTICLES = 0, MF_OUT_FIELDS = 1 };
@@ -104,10 +111,29 @@ int mf_ic_create(mf_ctx* ctx, const mf_ic_params* p, mf_ic** out);
 int mf_ic_destroy(mf_ic* ic);
 /* upload the real-space white noise (n^3 float64, host or device pointer) */
 int mf_ic_set_noise(mf_ic* ic, const double* noise, int location);
+/* generate the white noise on the device from a seed at the start of every
+ * run (the generator of mf_white_noise_host; no host field, no upload) */
+int mf_ic_set_noise_seed(mf_ic* ic, uint64_t seed);
+/* new cosmology scalars for the next run (same grid, box and order): the
+ * amplitude table, growth weights and velocity factors are recomputed on the
+ * device from a parameter block copied at the start of each run.  Not
+ * allowed when the pipeline was created with a tabulated T(k).  Call it only
+ * when no run of this pipeline is in flight. */
+int mf_ic_set_cosmology(mf_ic* ic, const mf_cosmo_scalars* cosmo);
 /* run noise -> phi(1..3), A(3) -> particles or fields into out (device
  * buffers of the ic when out->location is MF_LOC_DEVICE and out->pos is
- * NULL; copies to host buffers when MF_LOC_HOST) */
+ * NULL; copies to host buffers when MF_LOC_HOST); synchronous */
 int mf_ic_run(mf_ic* ic, mf_particles* out);
+/* enqueue the same pipeline on the context's stream and return without
+ * waiting; the particles stay in the ic's device buffers (mf_ic_particles).
+ * While the stream is being captured into a CUDA graph the work is recorded
+ * (requires mf_ic_set_noise_seed); a replay of the graph reruns the pipeline
+ * with the seed and cosmology set at replay time. */
+int mf_ic_enqueue(mf_ic* ic);
+/* device buffers of the particles (location MF_LOC_DEVICE) */
+int mf_ic_particles(mf_ic* ic, mf_particles* out);
+/* the context (and so the stream) the pipeline runs on */
+int mf_ic_context(mf_ic* ic, mf_ctx** out);
 /* per-stage device times of the last run in milliseconds:
  * [noise r2c + phi1, phi2, phi3, A3, positions, velocities, ids, d2h] */
 int mf_ic_stage_times(const mf_ic* ic, double* ms8);

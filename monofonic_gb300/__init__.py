@@ -152,6 +152,11 @@ class Grid_FFT:
         return self.download_padded().view(self.cdtype).reshape(self.n, self.n, self.n // 2 + 1).copy()
 
     # -- Grid_FFT methods ---------------------------------------------------
+    def fill_white_noise(self, seed: int):
+        """RNG_plugin::Fill_Grid (random_plugin.hh:37): the project plugin's
+        N(0,1) field generated on the device (bit-identical to the host plugin)"""
+        _check(self.ctx.ptr, lib().mf_grid_fill_white_noise(self.ptr, C.c_uint64(int(seed))))
+
     def FourierTransformForward(self, do_transform: bool = True):
         _check(self.ctx.ptr, lib().mf_grid_fft_forward(self.ptr, int(do_transform)))
 

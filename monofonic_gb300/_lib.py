@@ -114,6 +114,58 @@ SIGNATURES.update({
     "mf_ic_get_potential": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "mf_ic_get_noise": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "mf_plt_tables": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mf_grid_fill_white_noise": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "mf_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "mf_ic_set_noise_seed": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "mf_ic_set_cosmology": (C.c_int, [C.c_void_p, C.POINTER(mf_cosmo_scalars)]),
+    "mf_ic_enqueue": (C.c_int, [C.c_void_p]),
+    "mf_ic_particles": (C.c_int, [C.c_void_p, C.POINTER(mf_particles)]),
+    "mf_ic_context": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+})
+
+
+class mf_ic_request(C.Structure):
+    _fields_ = [("ngrid", C.c_int), ("boxlen", C.c_double), ("zstart", C.c_double), ("lpt_order", C.c_int),
+                ("lattice", C.c_int), ("precision", C.c_int), ("cosmo", mf_cosmo_params), ("seed", C.c_uint64),
+                ("pos64", C.c_int), ("id64", C.c_int)]
+
+
+MF_OUTPUT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int64, C.POINTER(mf_particles), C.c_int64, C.c_int64, C.c_int)
+
+
+class mf_server_config(C.Structure):
+    _fields_ = [("nworkers", C.c_int), ("hbm_budget", C.c_size_t), ("chunk_particles", C.c_int64),
+                ("output", MF_OUTPUT_FN), ("user", C.c_void_p), ("starvation_s", C.c_double)]
+
+
+class mf_request_result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("npart", C.c_int64), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_gpu_done", C.c_double), ("t_done", C.c_double), ("gpu_ms", C.c_double)]
+
+
+class mf_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("running", C.c_int64), ("bytes_in_use", C.c_size_t), ("bytes_budget", C.c_size_t),
+                ("peak_bytes", C.c_size_t), ("pooled_pipelines", C.c_int), ("t_now", C.c_double)]
+
+
+SIGNATURES.update({
+    "mf_batch_create": (C.c_int, [C.c_int, C.POINTER(mf_ic_request), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_batch_destroy": (C.c_int, [C.c_void_p]),
+    "mf_batch_set_items": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(mf_cosmo_params),
+                                     C.POINTER(C.c_uint64), C.c_int]),
+    "mf_batch_run": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "mf_batch_particles": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(mf_particles)]),
+    "mf_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_size_t)]),
+    "mf_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "mf_server_create": (C.c_int, [C.c_int, C.POINTER(mf_server_config), C.POINTER(C.c_void_p)]),
+    "mf_server_submit": (C.c_int, [C.c_void_p, C.POINTER(mf_ic_request), C.POINTER(C.c_int64)]),
+    "mf_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(mf_request_result), C.c_double]),
+    "mf_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
+    "mf_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(mf_server_stats)]),
+    "mf_server_now": (C.c_double, [C.c_void_p]),
+    "mf_server_last_error": (C.c_char_p, [C.c_void_p]),
+    "mf_server_destroy": (C.c_int, [C.c_void_p]),
 })
 
 _lib = None

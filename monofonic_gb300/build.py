@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmfgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 # extra compile definitions (tuning knobs such as -DMF_ZCONV_TMA_MAXR=4); a
 # different set builds into its own object directory
 EXTRA = os.environ.get("MF_NVCC_FLAGS", "").split()

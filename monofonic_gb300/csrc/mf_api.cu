@@ -37,7 +37,7 @@ int check_device_error(mf_ctx* c) {
 
 LaunchScope::LaunchScope(mf_ctx* c, int kind) : c_(c), kind_(kind) {
   ++c_->launches[kind];
-  if (c_->profile) {
+  if (c_->profile && !c_->capturing) {
     cudaEvent_t e0 = nullptr;
     if (c_->event_pool.size() >= 2) {
       e0 = c_->event_pool.back(); c_->event_pool.pop_back();
@@ -483,6 +483,23 @@ extern "C" int mf_grid_zero_dc(mf_grid* g) {
   return cuda_err(g->ctx, e, "mf_grid_zero_dc");
 }
 
+// RNG_plugin::Fill_Grid (include/random_plugin.hh:37) with the project
+// generator on the device; declared in monofonic_gb300_ic.h
+extern "C" int mf_grid_fill_white_noise(mf_grid* g, uint64_t seed) {
+  if (!g) return MF_ERR_ARG;
+  if (g->n & 1) return set_err(g->ctx, MF_ERR_SHAPE, "mf_grid_fill_white_noise: odd grid size");
+  cudaSetDevice(g->ctx->device);
+  cudaError_t e;
+  {
+    LaunchScope ls(g->ctx, KK_POINTWISE);
+    e = (g->prec == MF_PREC_F64) ? pw_white_noise<double>((double*)g->d, g->n, seed, nullptr, g->ctx->stream)
+                                 : pw_white_noise<float>((float*)g->d, g->n, seed, nullptr, g->ctx->stream);
+  }
+  if (e != cudaSuccess) return cuda_err(g->ctx, e, "mf_grid_fill_white_noise");
+  g->space = MF_SPACE_R;
+  return MF_OK;
+}
+
 extern "C" int mf_grid_inverse_laplacian(mf_grid* g) {
   if (!g) return MF_ERR_ARG;
   int rc = mf_grid_fft_forward(g, 1);
@@ -739,4 +756,9 @@ extern "C" int mf_host_alloc(size_t bytes, void** out) {
 extern "C" int mf_host_free(void* p) {
   if (p) cudaFreeHost(p);
   return MF_OK;
+}
+
+extern "C" int mf_copy_to_host(void* host, const void* device, size_t bytes) {
+  if (bytes && (!host || !device)) return MF_ERR_ARG;
+  return cudaMemcpy(host, device, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? MF_OK : MF_ERR_CUDA;
 }

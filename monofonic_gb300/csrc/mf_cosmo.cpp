@@ -22,6 +22,7 @@
 #include "../../include/monofonic_gb300_ic.h"
 #include "mf_cosmo.h"
 #include "mf_eh.cuh"
+#include "mf_noise.h"
 
 namespace mf {
 
@@ -262,25 +263,6 @@ double integrate_adaptive(const std::function<double(double)>& f, double a, doub
   return total;
 }
 
-inline uint32_t mulhilo(uint32_t a, uint32_t b, uint32_t* hi) {
-  const uint64_t p = (uint64_t)a * (uint64_t)b;
-  *hi = (uint32_t)(p >> 32);
-  return (uint32_t)p;
-}
-
-// Philox4x32-10 (Salmon, Moraes, Dror & Shaw 2011)
-inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
-  for (int r = 0; r < 10; ++r) {
-    uint32_t hi0, hi1;
-    const uint32_t lo0 = mulhilo(0xD2511F53u, c[0], &hi0);
-    const uint32_t lo1 = mulhilo(0xCD9E8D57u, c[2], &hi1);
-    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
-    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-}
-
 }  // namespace
 }  // namespace mf
 
@@ -352,19 +334,12 @@ extern "C" int mf_white_noise_host(int n, uint64_t seed, double* out, int nthrea
   if (n <= 0 || !out) return MF_ERR_ARG;
   const uint64_t ncell = (uint64_t)n * n * n, npair = (ncell + 1) / 2;
   if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
-  const uint32_t k0 = (uint32_t)(seed & 0xFFFFFFFFu), k1 = (uint32_t)(seed >> 32);
   auto work = [&](uint64_t p0, uint64_t p1) {
-    const double inv53 = 1.0 / 9007199254740992.0;
     for (uint64_t p = p0; p < p1; ++p) {
-      uint32_t c[4] = {(uint32_t)(p & 0xFFFFFFFFu), (uint32_t)(p >> 32), 0u, 0u};
-      philox4x32_10(c, k0, k1);
-      const uint64_t b1 = (((uint64_t)c[1] << 32) | c[0]) >> 11;
-      const uint64_t b2 = (((uint64_t)c[3] << 32) | c[2]) >> 11;
-      const double u1 = ((double)b1 + 0.5) * inv53, u2 = ((double)b2 + 0.5) * inv53;
-      const double r = std::sqrt(-2.0 * std::log(u1));
-      const double th = 2.0 * M_PI * u2;
-      out[2 * p] = r * std::cos(th);
-      if (2 * p + 1 < ncell) out[2 * p + 1] = r * std::sin(th);
+      double z0, z1;
+      noise::normal_pair(p, seed, &z0, &z1);
+      out[2 * p] = z0;
+      if (2 * p + 1 < ncell) out[2 * p + 1] = z1;
     }
   };
   std::vector<std::thread> th;

@@ -25,13 +25,22 @@ inline unsigned blocks_for(size_t n, int per = 4) {
   return (unsigned)(b ? b : 1);
 }
 
+// per-run parameters the kernels read from device memory, so that a pipeline
+// recorded once into a CUDA graph replays with a new cosmology and seed
+struct ICDyn {
+  EHParams eh;              // TFset_parameters of the cosmology
+  double half_ns, sqrtpnorm;
+  double w[2][4];           // positions / velocities: weights of phi, phi2, phi3 and the A3 term
+  unsigned long long seed;  // white-noise seed (device generator)
+};
+
 // amplitude table amp(k2) = k^{n_s/2} T(k) sqrt(pnorm), k = sqrt(k2)*kfac
 // (get_amplitude, include/cosmology_calculator.hh:405-408), FP64
-__global__ void k_amp_table(double* amp, int nk2, double kfac, double half_ns, double sqrtpnorm, EHParams eh,
-                            const double* tk) {
+__global__ void k_amp_table(double* amp, int nk2, double kfac, const ICDyn* __restrict__ dyn, const double* tk) {
+  const double half_ns = dyn->half_ns, sqrtpnorm = dyn->sqrtpnorm;
   for (int k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 < nk2; k2 += gridDim.x * blockDim.x) {
     const double k = sqrt((double)k2) * kfac;
-    const double t = tk ? tk[k2] : eh_eval(eh, k);
+    const double t = tk ? tk[k2] : eh_eval(dyn->eh, k);
     amp[k2] = pow(k, half_ns) * t * sqrtpnorm;
   }
 }
@@ -68,7 +77,8 @@ __global__ void k_phi1(cplx<T>* wn, cplx<T>* phi, int n, double kfac, const doub
 // :835-845 / :889-899) in FP64, stored in the grid precision
 template <typename T>
 __global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, const cplx<T>* p3, size_t tot,
-                         double w1, double w2, double w3) {
+                         const double* __restrict__ w) {
+  const double w1 = w[0], w2 = w[1], w3 = w[2];
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
     const cplx<T> a = p1[idx];
     double r = w1 * (double)a.x, im = w1 * (double)a.y;
@@ -149,7 +159,11 @@ struct mf_ic {
   size_t pos_bytes = 0, vel_bytes = 0, id_bytes = 0;
   int64_t npart = 0;
   cudaEvent_t ev[9] = {};
-  bool noise_set = false;
+  bool noise_set = false;   // an uploaded white-noise field is waiting in wn
+  bool noise_seeded = false; // the device generator fills wn at the start of each run
+  bool has_tk = false;      // amp + nk2 holds a tabulated T(k)
+  ICDyn* dyn_h = nullptr;   // page-locked host copy, copied to dyn_d at the start of each run
+  ICDyn* dyn_d = nullptr;
 };
 
 namespace {
@@ -183,14 +197,36 @@ void output_sizes(const mf_ic_params* p, int64_t* np, size_t* pb, size_t* vb, si
   *ib = (size_t)(*np) * (p->id64 ? 8 : 4);
 }
 
+// growth-factor weights of the two assembly passes (ic_generator.cc:221-234,
+// :835-845, :889-899): positions g_n, velocities n vfac g_n; the A3 term
+// carries g3c = D^3/7 (times 3 vfac for velocities)
+void fill_dyn(mf_ic* ic) {
+  const mf_ic_params& p = ic->p;
+  ICDyn& d = *ic->dyn_h;
+  eh_setup(p.cosmo.H0 > 0 ? p.cosmo.H0 : 100.0 * p.cosmo.h, p.cosmo.Omega_m, p.cosmo.Omega_b, p.cosmo.Tcmb, &d.eh);
+  d.half_ns = 0.5 * p.cosmo.n_s;
+  d.sqrtpnorm = std::sqrt(p.cosmo.pnorm);
+  const double D = p.cosmo.Dplus, vf = p.cosmo.vfac;
+  const double g1 = -D;
+  const double g2 = (p.lpt_order > 1) ? -3.0 / 7.0 * D * D : 0.0;
+  const double g3 = (p.lpt_order > 2) ? 1.0 / 3.0 * D * D * D : 0.0;
+  const double g3c = (p.lpt_order > 2) ? 1.0 / 7.0 * D * D * D : 0.0;
+  d.w[0][0] = g1; d.w[0][1] = g2; d.w[0][2] = g3; d.w[0][3] = g3c;
+  d.w[1][0] = vf * g1; d.w[1][1] = 2 * vf * g2; d.w[1][2] = 3 * vf * g3; d.w[1][3] = 3 * vf * g3c;
+}
+
+// the whole pipeline on the context's stream, without host synchronisation
+// or host-side data dependencies: safe to record into a CUDA graph once the
+// twiddle tables exist (mf_ic_create builds them)
 template <typename T>
-int run_impl(mf_ic* ic, mf_particles* out) {
+int enqueue_impl(mf_ic* ic) {
   mf_ctx* c = ic->ctx;
   cudaStream_t s = c->stream;
   const mf_ic_params& p = ic->p;
   const int n = p.ngrid, Kz = n / 2 + 1;
   const double L = p.boxlen, kfac = 2.0 * M_PI / L;
   const size_t nk = (size_t)n * n * Kz;
+  const bool timed = !c->capturing;
   cudaError_t e;
 #define CK(x)                                            \
   do {                                                   \
@@ -198,21 +234,19 @@ int run_impl(mf_ic* ic, mf_particles* out) {
     if (e != cudaSuccess) return cuda_err(c, e, #x);     \
   } while (0)
 
-  CK(cudaEventRecord(ic->ev[0], s));
-  // ---- white noise to k-space, phi(1) -----------------------------------
+  if (timed) CK(cudaEventRecord(ic->ev[0], s));
+  CK(cudaMemcpyAsync(ic->dyn_d, ic->dyn_h, sizeof(ICDyn), cudaMemcpyHostToDevice, s));
+  // ---- white noise (RNG_plugin::Fill_Grid) to k-space, phi(1) -----------------
+  if (ic->noise_seeded) {
+    LaunchScope ls(c, KK_POINTWISE);
+    CK(pw_white_noise<T>((T*)ic->wn->d, n, 0ull, &ic->dyn_d->seed, s));
+  }
   CK(fft3d_r2c<T>(c, (T*)ic->wn->d, n));
   ic->wn->space = MF_SPACE_K;
   {
-    EHParams eh;
-    eh_setup(p.cosmo.H0 > 0 ? p.cosmo.H0 : 100.0 * p.cosmo.h, p.cosmo.Omega_m, p.cosmo.Omega_b, p.cosmo.Tcmb, &eh);
-    const double* tk = nullptr;
-    if (p.tk_table) {
-      CK(cudaMemcpyAsync(ic->amp + ic->nk2, p.tk_table, sizeof(double) * ic->nk2, cudaMemcpyHostToDevice, s));
-      tk = ic->amp + ic->nk2;
-    }
     LaunchScope ls0(c, KK_POINTWISE);
-    k_amp_table<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ic->amp, ic->nk2, kfac, 0.5 * p.cosmo.n_s,
-                                                       std::sqrt(p.cosmo.pnorm), eh, tk);
+    k_amp_table<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ic->amp, ic->nk2, kfac, ic->dyn_d,
+                                                       ic->has_tk ? ic->amp + ic->nk2 : nullptr);
     CK(cudaGetLastError());
     const double volfac = std::pow(L / n / 2.0 / M_PI, 1.5);
     const double sgn = (p.inversion ? -1.0 : 1.0) / volfac;
@@ -222,7 +256,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
     CK(cudaGetLastError());
     ic->f[0]->space = MF_SPACE_K;
   }
-  CK(cudaEventRecord(ic->ev[1], s));
+  if (timed) CK(cudaEventRecord(ic->ev[1], s));
 
   auto H = [&](int g, int a, int b) {
     Operand<T> o{};
@@ -267,7 +301,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
     CK(conv2(H(0, 1, 2), H(0, 1, 2), 1, OUT_SUB, 1, 1));
     ic->f[1]->space = MF_SPACE_K;
   }
-  CK(cudaEventRecord(ic->ev[2], s));
+  if (timed) CK(cudaEventRecord(ic->ev[2], s));
   // ---- phi(3) (ic_generator.cc:511-528) ----------------------------------
   if (p.lpt_order > 2) {
     CK(conv3(H(0, 0, 0), H(0, 1, 1), H(0, 2, 2), 2, OUT_ASSIGN, 1));
@@ -283,7 +317,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
     CK(conv2(H(0, 1, 2), H(1, 1, 2), 2, OUT_AXPY, +10.0 / 7.0, 1));
     ic->f[2]->space = MF_SPACE_K;
   }
-  CK(cudaEventRecord(ic->ev[3], s));
+  if (timed) CK(cudaEventRecord(ic->ev[3], s));
   // ---- A(3) (ic_generator.cc:534-545) -----------------------------------
   if (p.lpt_order > 2) {
     for (int d = 0; d < 3; ++d) {
@@ -295,18 +329,10 @@ int run_impl(mf_ic* ic, mf_particles* out) {
       ic->f[tg]->space = MF_SPACE_K;
     }
   }
-  CK(cudaEventRecord(ic->ev[4], s));
+  if (timed) CK(cudaEventRecord(ic->ev[4], s));
 
-  // ---- growth factors (ic_generator.cc:221-234) ---------------------------
-  const double D = p.cosmo.Dplus;
-  const double g1 = -D;
-  const double g2 = (p.lpt_order > 1) ? -3.0 / 7.0 * D * D : 0.0;
-  const double g3 = (p.lpt_order > 2) ? 1.0 / 3.0 * D * D * D : 0.0;
-  const double g3c = (p.lpt_order > 2) ? 1.0 / 7.0 * D * D * D : 0.0;
-  const double vf = p.cosmo.vfac;
   const int overload = 1 << p.lattice;
   const bool fields = p.out_kind == MF_OUT_FIELDS;
-
   T* wsum = (T*)ic->wn->d;  // the noise grid is free after phi(1): holds the order sum
   const cplx<T>* P1 = (const cplx<T>*)ic->f[0]->d;
   const cplx<T>* P2 = ic->f[1] ? (const cplx<T>*)ic->f[1]->d : nullptr;
@@ -317,13 +343,10 @@ int run_impl(mf_ic* ic, mf_particles* out) {
   const size_t n3 = (size_t)n * n * n;
   for (int pass = 0; pass < 2; ++pass) {  // 0: positions, 1: velocities
     const bool vel = pass == 1;
-    // weights: positions g_n; velocities vfac_n g_n with vfac_n = n vfac
-    const double w1 = vel ? vf * g1 : g1, w2 = vel ? 2 * vf * g2 : g2, w3 = vel ? 3 * vf * g3 : g3;
-    const double wA = vel ? 3 * vf * g3c : g3c;
     {
       LaunchScope ls(c, KK_POINTWISE);
       k_phitot<T><<<blocks_for(nk), kThreads, 0, s>>>((cplx<T>*)wsum, P1, p.lpt_order > 1 ? P2 : nullptr,
-                                                     p.lpt_order > 2 ? P3 : nullptr, nk, w1, w2, w3);
+                                                     p.lpt_order > 2 ? P3 : nullptr, nk, ic->dyn_d->w[pass]);
     }
     CK(cudaGetLastError());
     void* dst = vel ? ic->dvel : ic->dpos;
@@ -346,7 +369,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
           for (int q = 0; q < 3; ++q)
             op.s2[st - 1][q] = (int)lround(2 * (kShifts[p.lattice][st][q] - kShifts[p.lattice][st - 1][q]));
         op.kfac = T(kfac);
-        op.wA = T(wA);
+        op.wA = &ic->dyn_d->w[pass][3];
         op.unit = T((vel ? p.vunit : p.lunit) / L);
         op.plt = p.plt;
         op.vel = vel ? 1 : 0;
@@ -388,7 +411,7 @@ int run_impl(mf_ic* ic, mf_particles* out) {
         k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, qt, vel ? 0 : 1, 0);
       CK(cudaGetLastError());
     }
-    CK(cudaEventRecord(ic->ev[5 + pass], s));
+    if (timed) CK(cudaEventRecord(ic->ev[5 + pass], s));
   }
   // ---- particle IDs (particle_generator.hh:212-253) ------------------------
   if (!fields) {
@@ -399,8 +422,22 @@ int run_impl(mf_ic* ic, mf_particles* out) {
       k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->dids, n, overload, 0);
     CK(cudaGetLastError());
   }
-  CK(cudaEventRecord(ic->ev[7], s));
-  // ---- hand-off ---------------------------------------------------------------
+  if (timed) CK(cudaEventRecord(ic->ev[7], s));
+#undef CK
+  return MF_OK;
+}
+
+// hand-off of the particles (device pointers, or copies into host buffers)
+int handoff(mf_ic* ic, mf_particles* out) {
+  mf_ctx* c = ic->ctx;
+  cudaStream_t s = c->stream;
+  const bool fields = ic->p.out_kind == MF_OUT_FIELDS;
+  cudaError_t e;
+#define CK(x)                                            \
+  do {                                                   \
+    e = (x);                                             \
+    if (e != cudaSuccess) return cuda_err(c, e, #x);     \
+  } while (0)
   if (out) {
     out->npart = ic->npart;
     if (out->location == MF_LOC_HOST) {
@@ -415,7 +452,6 @@ int run_impl(mf_ic* ic, mf_particles* out) {
     }
   }
   CK(cudaEventRecord(ic->ev[8], s));
-  CK(cudaStreamSynchronize(s));
 #undef CK
   return MF_OK;
 }
@@ -475,6 +511,8 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->dids);
   for (auto& e : ic->ev)
     if (e) cudaEventDestroy(e);
+  cudaFree(ic->dyn_d);
+  cudaFreeHost(ic->dyn_h);
   --c->children;
   delete ic;
   return MF_OK;
@@ -557,6 +595,28 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   ic->nk2 = 3 * (n / 2) * (n / 2) + 1;
   cudaError_t e = cudaMalloc(&ic->amp, sizeof(double) * 2 * ic->nk2);
   if (e != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: amplitude table"));
+  if (p->tk_table) {  // tabulated T(k) of any transfer plugin, one value per integer k^2
+    e = cudaMemcpy(ic->amp + ic->nk2, p->tk_table, sizeof(double) * ic->nk2, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: T(k) table"));
+    ic->has_tk = true;
+  }
+  if ((e = cudaHostAlloc((void**)&ic->dyn_h, sizeof(ICDyn), cudaHostAllocDefault)) != cudaSuccess)
+    return fail(cuda_err(c, e, "mf_ic_create: parameter block"));
+  std::memset(ic->dyn_h, 0, sizeof(ICDyn));
+  if ((e = cudaMalloc((void**)&ic->dyn_d, sizeof(ICDyn))) != cudaSuccess)
+    return fail(cuda_err(c, e, "mf_ic_create: parameter block"));
+  fill_dyn(ic);
+  // twiddle tables of every length the pipeline uses, built now so that a
+  // run can be recorded into a graph
+  {
+    const int M = (p->convolver == MF_CONV_ORSZAG) ? 3 * n / 2 : n;
+    const int lens[4] = {n, n / 2, M, M / 2};
+    for (int L : lens) {
+      const void* t = (p->precision == MF_PREC_F32) ? (const void*)c->tw.get<float>(L, c->stream)
+                                                     : (const void*)c->tw.get<double>(L, c->stream);
+      if (!t) return fail(set_err(c, MF_ERR_OOM, "mf_ic_create: twiddle tables"));
+    }
+  }
   output_sizes(p, &ic->npart, &ic->pos_bytes, &ic->vel_bytes, &ic->id_bytes);
   if ((e = cudaMalloc(&ic->dpos, ic->pos_bytes)) != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: positions"));
   if ((e = cudaMalloc(&ic->dvel, ic->vel_bytes)) != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: velocities"));
@@ -590,17 +650,69 @@ extern "C" int mf_ic_set_noise(mf_ic* ic, const double* noise, int location) {
   if (e != cudaSuccess) return cuda_err(c, e, "mf_ic_set_noise");
   ic->wn->space = MF_SPACE_R;
   ic->noise_set = true;
+  ic->noise_seeded = false;
   return MF_OK;
+}
+
+extern "C" int mf_ic_set_noise_seed(mf_ic* ic, uint64_t seed) {
+  if (!ic) return MF_ERR_ARG;
+  ic->dyn_h->seed = (unsigned long long)seed;
+  ic->noise_seeded = true;
+  ic->noise_set = false;
+  return MF_OK;
+}
+
+extern "C" int mf_ic_set_cosmology(mf_ic* ic, const mf_cosmo_scalars* cosmo) {
+  if (!ic || !cosmo) return MF_ERR_ARG;
+  if (!(cosmo->pnorm > 0) || !(cosmo->Dplus > 0)) return set_err(ic->ctx, MF_ERR_ARG, "mf_ic_set_cosmology: bad scalars");
+  if (ic->has_tk) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_set_cosmology: the pipeline uses a tabulated T(k)");
+  ic->p.cosmo = *cosmo;
+  fill_dyn(ic);
+  return MF_OK;
+}
+
+extern "C" int mf_ic_enqueue(mf_ic* ic) {
+  if (!ic) return MF_ERR_ARG;
+  mf_ctx* c = ic->ctx;
+  cudaSetDevice(c->device);
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(c->stream, &st);
+  if (e != cudaSuccess) return cuda_err(c, e, "mf_ic_enqueue: capture status");
+  const bool cap = (st == cudaStreamCaptureStatusActive);
+  if (cap && !ic->noise_seeded)
+    return set_err(c, MF_ERR_STATE, "mf_ic_enqueue: a recorded pipeline needs the device noise generator (mf_ic_set_noise_seed)");
+  if (!ic->noise_set && !ic->noise_seeded) return set_err(c, MF_ERR_STATE, "mf_ic_enqueue: white noise not set");
+  c->capturing = cap;
+  const int rc = (ic->p.precision == MF_PREC_F64) ? enqueue_impl<double>(ic) : enqueue_impl<float>(ic);
+  c->capturing = false;
+  if (!cap) ic->noise_set = false;  // the uploaded grid is consumed (transformed in place)
+  return rc;
 }
 
 extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
-  if (!ic->noise_set) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
-  cudaSetDevice(ic->ctx->device);
-  int rc = (ic->p.precision == MF_PREC_F64) ? run_impl<double>(ic, out) : run_impl<float>(ic, out);
-  ic->noise_set = false;  // the noise grid is consumed (transformed and normalised in place)
+  if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
+  int rc = mf_ic_enqueue(ic);
+  if (rc == MF_OK) rc = handoff(ic, out);
   if (rc == MF_OK) rc = check_device_error(ic->ctx);
+  else cudaStreamSynchronize(ic->ctx->stream);
   return rc;
+}
+
+extern "C" int mf_ic_particles(mf_ic* ic, mf_particles* out) {
+  if (!ic || !out) return MF_ERR_ARG;
+  out->pos = ic->dpos;
+  out->vel = ic->dvel;
+  out->ids = ic->dids;
+  out->npart = ic->npart;
+  out->location = MF_LOC_DEVICE;
+  return MF_OK;
+}
+
+extern "C" int mf_ic_context(mf_ic* ic, mf_ctx** out) {
+  if (!ic || !out) return MF_ERR_ARG;
+  *out = ic->ctx;
+  return MF_OK;
 }
 
 extern "C" int mf_ic_stage_times(const mf_ic* ic, double* ms) {

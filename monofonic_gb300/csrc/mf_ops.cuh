@@ -257,7 +257,8 @@ struct AssembleXInvOp {
   // particle_generator.hh:505-522), each 2*(s_ish - s_{ish-1}) in {-1,0,1}
   int nstep;
   int s2[7][3];
-  T kfac, wA, unit;
+  T kfac, unit;
+  const double* wA;  // device scalar: weight of the A3 term (growth factor of this pass)
   int plt;          // PLT corrected gradient (lattice_gradient, particle_plt.hh:551-573)
   int vel;          // velocities: times the PLT growth-rate correction vfac_corr (:575-585)
   PLTDev<T> P;
@@ -285,8 +286,9 @@ struct AssembleXInvOp {
     T rr = -gd * P1.y, ri = gd * P1.x;
     if (A3p) {
       const C X1 = A3pp[idx], X2 = A3p[idx];
-      rr += wA * (-(gp * X1.y) + gpp * X2.y);
-      ri += wA * (gp * X1.x - gpp * X2.x);
+      const T w = T(__ldg(wA));
+      rr += w * (-(gp * X1.y) + gpp * X2.y);
+      ri += w * (gp * X1.x - gpp * X2.x);
     }
     if (plt && vel) {
       rr *= vc;

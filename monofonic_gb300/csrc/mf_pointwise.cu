@@ -1,6 +1,7 @@
 // Pointwise k-space / real-space kernels on N-grids (padded in-place layout).
 #include <cmath>
 
+#include "mf_noise.h"
 #include "mf_runtime.h"
 
 namespace mf {
@@ -39,6 +40,29 @@ __global__ void k_invlap(cplx<T>* d, int n, T kfac) {
     const T k2 = kx * kx + ky * ky + kk * kk;
     cplx<T> v = d[idx];
     d[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(-v.x / k2, -v.y / k2);
+  }
+}
+
+// white noise of the project RNG plugin on the device (the generator of
+// mf_noise.h, the same bits as the host plugin), written into the padded
+// real layout; pair p = cells 2p, 2p+1 of one z row (n even).  The seed is
+// read from device memory when seed_dev is given (replayable graphs).
+template <typename T>
+__global__ void k_white_noise(T* d, int n, unsigned long long seed, const unsigned long long* seed_dev) {
+  using T2 = typename cplx_of<T>::type;
+  const unsigned long long sd = seed_dev ? *seed_dev : seed;
+  const unsigned hn = (unsigned)n >> 1;
+  const unsigned long long npair = (unsigned long long)n * n * hn;
+  for (unsigned long long p = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; p < npair;
+       p += (unsigned long long)gridDim.x * blockDim.x) {
+    double z0, z1;
+    noise::normal_pair(p, sd, &z0, &z1);
+    const unsigned long long line = p / hn;
+    const unsigned k = 2u * (unsigned)(p - line * hn);
+    T2 v;
+    v.x = (T)z0;
+    v.y = (T)z1;
+    *reinterpret_cast<T2*>(d + line * (unsigned long long)(n + 2) + k) = v;
   }
 }
 
@@ -128,6 +152,12 @@ cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s) {
   return cudaGetLastError();
 }
 template <typename T>
+cudaError_t pw_white_noise(T* d, int n, unsigned long long seed, const unsigned long long* seed_dev, cudaStream_t s) {
+  if (n <= 0 || (n & 1)) return cudaErrorInvalidValue;
+  k_white_noise<T><<<grid_for((size_t)n * n * (n / 2), 2), kThreads, 0, s>>>(d, n, seed, seed_dev);
+  return cudaGetLastError();
+}
+template <typename T>
 cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, double* acc, cudaStream_t s) {
   const size_t smem = (size_t)4 * nbins * sizeof(double);
   if (smem > 48 * 1024) {
@@ -144,6 +174,7 @@ cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, d
   template cudaError_t pw_invlap<T>(cplx<T>*, int, double, cudaStream_t);                            \
   template cudaError_t pw_shift<T>(cplx<T>*, int, double, double, const double*, cudaStream_t);      \
   template cudaError_t pw_fill_from_f64<T>(T*, const double*, int, cudaStream_t);                    \
+  template cudaError_t pw_white_noise<T>(T*, int, unsigned long long, const unsigned long long*, cudaStream_t); \
   template cudaError_t pw_power_spectrum<T>(const cplx<T>*, int, double, int, double*, cudaStream_t);
 INST(float)
 INST(double)

@@ -31,6 +31,7 @@ struct mf_ctx {
   std::string err;
   int children = 0;  // live grids, convolvers and pipelines on this context
   int* d_err = nullptr;  // device error flag set by bounded waits in kernels
+  bool capturing = false;  // work is being recorded into a CUDA graph (no profiling events)
   // launch accounting
   long long launches[mf::KK_COUNT] = {};
   bool profile = false;
@@ -101,6 +102,10 @@ template <typename T> cudaError_t pw_zero_dc(T* d, cudaStream_t s);
 template <typename T> cudaError_t pw_invlap(cplx<T>* d, int n, double kfac, cudaStream_t s);
 template <typename T> cudaError_t pw_shift(cplx<T>* d, int n, double kfac, double dx, const double sh[3], cudaStream_t s);
 template <typename T> cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s);
+// project RNG plugin on the device (bit-identical to mf_white_noise_host);
+// seed from *seed_dev when it is not null
+template <typename T>
+cudaError_t pw_white_noise(T* d, int n, unsigned long long seed, const unsigned long long* seed_dev, cudaStream_t s);
 template <typename T>
 cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, double* acc /*4*nbins*/, cudaStream_t s);
 

@@ -129,6 +129,16 @@ class ICGenerator:
     def set_noise_device(self, dptr: int):
         _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, C.c_void_p(dptr), L.MF_LOC_DEVICE))
 
+    def set_noise_seed(self, seed: int):
+        """white noise of the project RNG plugin generated on the device at
+        the start of every run (the same bits as white_noise(n, seed))"""
+        _check(self.ctx.ptr, lib().mf_ic_set_noise_seed(self.ptr, C.c_uint64(int(seed))))
+
+    def set_cosmology(self, scalars):
+        """new cosmology scalars (cosmology_scalars) for the next run"""
+        _check(self.ctx.ptr, lib().mf_ic_set_cosmology(self.ptr, C.byref(scalars)))
+        self.params.cosmo = scalars
+
     def set_noise_host_ptr(self, hptr: int):
         """noise from a host pointer (e.g. page-locked memory of mf_host_alloc)."""
         _check(self.ctx.ptr, lib().mf_ic_set_noise(self.ptr, C.c_void_p(hptr), L.MF_LOC_HOST))

@@ -108,3 +108,13 @@ def test_host_noise_matches_oracle(mflib):
     for n in (8, 16, 33 - 1):
         a = ic.white_noise(n, 2024, nthreads=3)
         assert np.allclose(a, O.white_noise(n, 2024), rtol=1e-14, atol=1e-14)
+
+
+def test_host_noise_golden_fixture(mflib):
+    """the project RNG plugin reproduces the committed field bit for bit, on
+    any thread count, and agrees with the oracle's libm restatement"""
+    from monofonic_gb300 import ic
+    ref = np.load(os.path.join(ROOT, "tests", "golden", "noise_n16_seed12345.npy"))
+    for nt in (1, 4):
+        assert np.array_equal(ic.white_noise(16, 12345, nthreads=nt), ref)
+    assert np.allclose(ref, O.white_noise(16, 12345), rtol=1e-14, atol=1e-14)
