@@ -103,40 +103,95 @@ __device__ __forceinline__ void dft8(cplx<T>* a) {
   a[3] = cadd(e3, w3); a[7] = csub(e3, w3);
 }
 
+__host__ __device__ constexpr int inv_mod(int a, int m) {
+  for (int x = 1; x < m; ++x)
+    if ((a * x) % m == 1) return x;
+  return 1;
+}
+
+template <typename T, bool INV, int R>
+__device__ __forceinline__ void dftR(cplx<T>* a);
+
+// DFT of size R = R1 R2 with gcd(R1, R2) = 1 by the Good-Thomas prime-factor
+// mapping: input n = (n1 R2 + n2 R1) mod R, output k = (k1 R2 u + k2 R1 v)
+// mod R with u = R2^-1 mod R1, v = R1^-1 mod R2; a DFT-R1 over n1, then a
+// DFT-R2 over n2, and no twiddle factors in between.  All indices are
+// compile-time, so the permutations are register renamings.
+template <typename T, bool INV, int R1, int R2>
+__device__ __forceinline__ void dft_pfa(cplx<T>* a) {
+  constexpr int R = R1 * R2;
+  constexpr int U = inv_mod(R2, R1), V = inv_mod(R1, R2);
+  cplx<T> t[R];
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2)
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) t[n2 * R1 + n1] = a[(n1 * R2 + n2 * R1) % R];
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) dftR<T, INV, R1>(&t[n2 * R1]);
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) {
+    cplx<T> s[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) s[n2] = t[n2 * R1 + k1];
+    dftR<T, INV, R2>(s);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) a[(k1 * R2 * U + k2 * R1 * V) % R] = s[k2];
+  }
+}
+
 template <typename T, bool INV, int R>
 __device__ __forceinline__ void dftR(cplx<T>* a) {
   if constexpr (R == 2) dft2<T, INV>(a);
   else if constexpr (R == 3) dft3<T, INV>(a);
   else if constexpr (R == 4) dft4<T, INV>(a);
   else if constexpr (R == 8) dft8<T, INV>(a);
+  else if constexpr (R == 6) dft_pfa<T, INV, 2, 3>(a);
+  else if constexpr (R == 12) dft_pfa<T, INV, 4, 3>(a);
   else static_assert(R == 2, "unsupported radix");
 }
 
 // ---------------------------------------------------------------------------
-// compile-time plans: L -> radix list (8s first, then 4/2, then 3s)
+// compile-time plans: L -> radix list.  maxr >= 8: as many radix-8 stages as
+// the power of two allows, the remaining factor 2 or 4 merged with one factor
+// 3 into a radix-6 or radix-12 stage (when MF_FFT_COMPOSITE), then the other
+// 3s; maxr 4: radix 4/2 stages, then 3s.  Merging keeps E = lcm(radices)
+// unchanged and removes one shared-memory exchange.
 // ---------------------------------------------------------------------------
+#ifndef MF_FFT_COMPOSITE
+#define MF_FFT_COMPOSITE 1
+#endif
 __host__ __device__ constexpr int ilog2_part(int L) { int a = 0; while (L % 2 == 0) { L /= 2; ++a; } return a; }
 __host__ __device__ constexpr int i3_part(int L) { int b = 0; while (L % 3 == 0) { L /= 3; ++b; } return b; }
 __host__ __device__ constexpr bool plan_ok(int L) {
   int x = L; while (x % 2 == 0) x /= 2; while (x % 3 == 0) x /= 3; return x == 1 && L >= 4;
 }
-__host__ __device__ constexpr int plan_nstages(int L, int maxr) {
-  int a = ilog2_part(L), b = i3_part(L), n = b;
-  int r8 = (maxr >= 8) ? a / 3 : 0;
-  int rem = a - 3 * r8;
-  n += r8;
-  while (rem > 0) { int t = (rem >= 2 && maxr >= 4) ? 2 : 1; rem -= t; ++n; }
-  return n;
-}
-__host__ __device__ constexpr int plan_radix(int L, int maxr, int s) {
+struct FFTPlan {
+  int n = 0;
+  int r[16] = {};
+};
+__host__ __device__ constexpr FFTPlan make_plan(int L, int maxr) {
+  FFTPlan p{};
   int a = ilog2_part(L), b = i3_part(L);
-  int r8 = (maxr >= 8) ? a / 3 : 0;
-  int rem = a - 3 * r8;
-  int idx = 0;
-  for (int i = 0; i < r8; ++i) { if (idx == s) return 8; ++idx; }
-  while (rem > 0) { int t = (rem >= 2 && maxr >= 4) ? 2 : 1; rem -= t; if (idx == s) return 1 << t; ++idx; }
-  for (int i = 0; i < b; ++i) { if (idx == s) return 3; ++idx; }
-  return 1;
+  if (maxr >= 8) {
+    const int r8 = a / 3;
+    int rem = a - 3 * r8;
+    for (int i = 0; i < r8; ++i) p.r[p.n++] = 8;
+    if (MF_FFT_COMPOSITE && rem > 0 && b > 0) {
+      p.r[p.n++] = (rem == 1) ? 6 : 12;
+      rem = 0;
+      --b;
+    }
+    while (rem > 0) { const int t = (rem >= 2) ? 2 : 1; rem -= t; p.r[p.n++] = 1 << t; }
+  } else {
+    while (a > 0) { const int t = (a >= 2 && maxr >= 4) ? 2 : 1; a -= t; p.r[p.n++] = 1 << t; }
+  }
+  for (int i = 0; i < b; ++i) p.r[p.n++] = 3;
+  return p;
+}
+__host__ __device__ constexpr int plan_nstages(int L, int maxr) { return make_plan(L, maxr).n; }
+__host__ __device__ constexpr int plan_radix(int L, int maxr, int s) {
+  const FFTPlan p = make_plan(L, maxr);
+  return (s < p.n) ? p.r[s] : 1;
 }
 __host__ __device__ constexpr int plan_elems(int L, int maxr) {
   // lcm of the radices
