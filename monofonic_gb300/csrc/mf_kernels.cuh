@@ -13,10 +13,18 @@
 //                 HBM; real transforms use the half-length complex packing.
 #pragma once
 
+#include <type_traits>
+
 #include "mf_fft.cuh"
 #include "mf_tma.cuh"
 
 namespace mf {
+
+// ops with a per-tile prologue (tile_prep / xform_tile) in the pipelined pass
+template <class OP, class = void>
+struct has_tile_prep : std::false_type {};
+template <class OP>
+struct has_tile_prep<OP, std::void_t<decltype(&OP::tile_prep)>> : std::true_type {};
 
 // ---------------------------------------------------------------------------
 // strided column pass
@@ -107,10 +115,19 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
     const int col = ct * NCOL + c;
     const bool valid = col < ncols;
     C v[F::E];
+    if constexpr (has_tile_prep<OP>::value) {
+      const auto tp = op.tile_prep(z, slab, col);
 #pragma unroll
-    for (int s = 0; s < F::E; ++s) {
-      const int e = F::in_index(t, s);
-      v[s] = valid ? op.xform(z, slab, e, col, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+      for (int s = 0; s < F::E; ++s) {
+        const int e = F::in_index(t, s);
+        v[s] = valid ? op.xform_tile(tp, e, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) {
+        const int e = F::in_index(t, s);
+        v[s] = valid ? op.xform(z, slab, e, col, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+      }
     }
     if constexpr (OP::kPrefetch) {
       C pre[F::E];

@@ -124,6 +124,51 @@ struct ConvXInvOp {
     const C v = operand_value<T>(kind, dsel<0>(z), dsel<1>(z), dsel<2>(z), dsel<3>(z), v0, i, j, kz, g.N, kfac);
     return mkc<T>(v.x * scale, v.y * scale);
   }
+  // per-tile form: along x only g_i varies, so the operand factor (times the
+  // scale) is the polynomial c0 + c1 g_i + c2 g_i^2 with coefficients fixed
+  // by the operand kind, its directions, g_j and g_kz; GRAD multiplies by
+  // i (c0 + c1 g_i)
+  struct Tile {
+    T c0, c1, c2;
+    bool grad;
+  };
+  __device__ __forceinline__ Tile tile_prep(int z, int j, int kz) const {
+    const int kind = z == 0 ? opnd[0].kind : (z == 1 ? opnd[1].kind : opnd[2].kind);
+    const int d[4] = {dsel<0>(z), dsel<1>(z), dsel<2>(z), dsel<3>(z)};
+    const T gj = gradk<T>(j, g.N, kfac), gk = gradk<T>(kz, g.N, kfac);
+    auto gof = [&](int a) { return a == 1 ? gj : gk; };
+    Tile t{T(0), T(0), T(0), false};
+    auto term = [&](int a, int b, T sgn) {  // adds sgn * (-g_a g_b)
+      const int m = (a == 0) + (b == 0);
+      if (m == 2) t.c2 -= sgn;
+      else if (m == 1) t.c1 -= sgn * gof(a == 0 ? b : a);
+      else t.c0 -= sgn * gof(a) * gof(b);
+    };
+    if (kind == OPND_PLAIN) {
+      t.c0 = T(1);
+    } else if (kind == OPND_GRAD) {
+      t.grad = true;
+      if (d[0] == 0) t.c1 = T(1);
+      else t.c0 = gof(d[0]);
+    } else {
+      term(d[0], d[1], T(1));
+      if (kind == OPND_SUM) term(d[2], d[3], T(1));
+      if (kind == OPND_DIFF) term(d[2], d[3], T(-1));
+    }
+    t.c0 *= scale;
+    t.c1 *= scale;
+    t.c2 *= scale;
+    return t;
+  }
+  __device__ __forceinline__ C xform_tile(const Tile& t, int x, C v0) const {
+    const T gi = gradk<T>(g.src_row(x), g.N, kfac);
+    if (t.grad) {
+      const T f = t.c1 * gi + t.c0;
+      return mkc<T>(-f * v0.y, f * v0.x);
+    }
+    const T f = (t.c2 * gi + t.c1) * gi + t.c0;
+    return mkc<T>(v0.x * f, v0.y * f);
+  }
   __device__ __forceinline__ void store_z(int z, int j, int x, int kz, C v) const {
     C* d = z == 0 ? dst[0] : (z == 1 ? dst[1] : dst[2]);
     d[((long long)x * g.M + j) * g.Kz + kz] = v;
