@@ -40,6 +40,9 @@ template <typename C, typename T>
 __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
 template <typename C>
 __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+// correctly rounded reciprocal (IEEE round-to-nearest)
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, typename C>
 __device__ __forceinline__ C cmul_mi(C a) { C r; if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; } return r; }

@@ -270,7 +270,8 @@ struct ConvXFwdOp {
     if (post_invlap) {
       const T kx = kcomp<T>(i, g.N, kfac), ky = kcomp<T>(j, g.N, kfac), kzz = kcomp<T>(kz, g.N, kfac);
       const T k2 = kx * kx + ky * ky + kzz * kzz;
-      r = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(-r.x / k2, -r.y / k2);
+      const T m = -rcp_rn(k2);
+      r = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(r.x * m, r.y * m);
     }
     target[idx] = r;
   }

@@ -4,6 +4,8 @@
 #include <cmath>
 #include <cstddef>
 
+#include "mf_fft.cuh"
+
 namespace mf {
 
 // device copy of the tables in one precision
@@ -27,7 +29,8 @@ __device__ __forceinline__ T plt_cic(const T* __restrict__ tab, int ng, T x, T y
   const T dx = x - T(ix), tx = T(1) - dx;
   const T dy = y - T(iy), ty = T(1) - dy;
   const T dz = z - T(iz), tz = T(1) - dz;
-  const int ix1 = (ix + 1) % ng, iy1 = (iy + 1) % ng, iz1 = min(iz + 1, nk - 1);
+  // x, y in [0, ng): the periodic neighbour wraps only at the last index
+  const int ix1 = (ix + 1 == ng) ? 0 : ix + 1, iy1 = (iy + 1 == ng) ? 0 : iy + 1, iz1 = min(iz + 1, nk - 1);
   auto at = [&](int a, int b, int k) { return tab[((size_t)a * ng + b) * nk + k]; };
   T v = T(0);
   v += at(ix, iy, iz) * tx * ty * tz;
@@ -60,11 +63,13 @@ __device__ __forceinline__ void plt_gradient(const PLTDev<T>& P, int i, int j, i
   T st = T(0), ct = T(1), sp = T(0), cp = T(1);
   if (kr > T(0)) {
     const T kp = sqrt(kx * kx + ky * ky);
-    st = kp / kr;
-    ct = kz2 / kr;
+    const T ir = rcp_rn(kr);
+    st = kp * ir;
+    ct = kz2 * ir;
     if (kp > T(0)) {
-      sp = ky / kp;
-      cp = kx / kp;
+      const T ip = rcp_rn(kp);
+      sp = ky * ip;
+      cp = kx * ip;
     }
   }
   g[0] = kmod * (Dr * st * cp + Dt * ct * cp - Dp * sp);
