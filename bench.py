@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-items", type=int, default=96)
     ap.add_argument("--batch-streams", type=int, default=8)
@@ -242,6 +243,15 @@ def _draw_request(rng, sizes, prec):
                    lattice="sc", precision=prec, cosmology=_draw_cosmology(rng), seed=int(rng.integers(1, 2 ** 62)))
 
 
+def _tuning_summary(report: str) -> dict:
+    """{"conv_xinv L=768 f32": "occ 0", ...} from an autotuner report"""
+    out = {}
+    for line in report.splitlines():
+        if ":" in line and "->" in line:
+            out[line.split(":")[0]] = line.split("->")[1].strip()
+    return out
+
+
 def _pct(xs, q):
     xs = sorted(xs)
     return xs[min(len(xs) - 1, max(0, int(math.ceil(q * len(xs))) - 1))]
@@ -258,8 +268,9 @@ def run_batch(args, device):
     rng = np.random.default_rng(2024)
     reqs = [_draw_request(rng, BATCH_SIZES, "f32") for _ in range(args.batch_items)]
     t0 = time.perf_counter()
-    b = Batch(reqs, nstreams=args.batch_streams, device=device)
+    b = Batch(reqs, nstreams=args.batch_streams, device=device, autotune=not args.no_autotune)
     t_create = time.perf_counter() - t0
+    tuning = _tuning_summary(b.tuning)
     info = b.info()
     for _ in range(max(3, args.warmup)):
         b.run()
@@ -283,7 +294,8 @@ def run_batch(args, device):
             "device_GB": round(info["device_bytes"] / 1e9, 2), "create_s": round(t_create, 2),
             "ms_per_batch": ms, "ms_per_batch_max": max(dev_ms),
             "realizations_per_s": len(reqs) / (ms / 1e3), "particles_per_s": npart / (ms / 1e3),
-            "host_cosmology_ms": statistics.median(host_ms)}
+            "host_cosmology_ms": statistics.median(host_ms),
+            "autotuned_schedules": tuning}
 
 
 def run_serve(args, device, prec, seconds):
@@ -426,6 +438,13 @@ def run_mf(args):
         names = ["noise_r2c+phi1", "phi2", "phi3", "A3", "positions", "velocities", "ids", "handoff"]
         return dict(zip(names, [round(x, 3) for x in gen.stage_times()]))
 
+    # ---- schedules chosen by the autotuner (process-wide) ------------------------
+    tuned = {}
+    if not args.no_autotune:
+        tuned["f32"] = _tuning_summary(ic.autotune(ctx, n, "f32"))
+        if not args.no_fp64:
+            tuned["f64"] = _tuning_summary(ic.autotune(ctx, n, "f64"))
+
     # ---- FP32-bulk, inputs resident ------------------------------------------
     gen32 = make("f32")
     npart = gen32.npart
@@ -533,6 +552,7 @@ def run_mf(args):
                          "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"},
             "kernels": kinds,
             "stages_ms": stages32,
+            "autotuned_schedules": tuned or None,
             "e2e": e2e,
             "fp64_plain": fp64,
             "cpu_baseline": cpu,

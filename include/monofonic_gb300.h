@@ -86,6 +86,22 @@ int mf_host_free(void* p);
 /* synchronous copy of device memory (e.g. particles of mf_ic_particles) to
  * host memory (no reference counterpart) */
 int mf_copy_to_host(void* host, const void* device, size_t bytes);
+/* autotuner (no reference counterpart; the reference's FFTW planning,
+ * src/grid_fft.cc:50-62, plays the same role for its CPU transforms): times
+ * the candidate schedules of the five convolution passes for grid size n in
+ * precision prec (persistent CTAs per SM; z-pass kernel and radix plan) on a
+ * scratch convolution and keeps the fastest in a process-wide table that every
+ * later launch of those passes uses.  report (optional) receives one line per
+ * pass kind.  Tune before recording graphs: the table is read at launch. */
+int mf_autotune(mf_ctx* ctx, int n, int prec, char* report, size_t report_len);
+/* back to the compiled default schedules */
+int mf_autotune_reset(void);
+/* set one entry of that table by hand: pass kind (0 conv_xinv, 1 conv_yinv,
+ * 2 conv_z, 3 conv_yfwd, 4 conv_xfwd), transform length L (3N/2 for the
+ * Orszag convolver), precision, persistent CTAs per SM (0: occupancy limit)
+ * and, for conv_z, the kernel (0 TMA-pipelined radix-8 plan, 1 direct-load
+ * radix-4 plan) */
+int mf_schedule_set(int kind, int L, int prec, int occ, int variant);
 /* 1 if grid size n is supported by the compiled kernels */
 int mf_grid_size_supported(int n);
 

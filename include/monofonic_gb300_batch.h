@@ -42,7 +42,10 @@ typedef struct {
  * graph launch.  New seeds and cosmologies replay the same graph. */
 typedef struct mf_batch mf_batch;
 
-int mf_batch_create(int device, const mf_ic_request* items, int nitems, int nstreams, mf_batch** out);
+enum { MF_BATCH_AUTOTUNE = 1 };
+/* flags: MF_BATCH_AUTOTUNE runs mf_autotune for every distinct grid size and
+ * precision of the batch before the graph is recorded */
+int mf_batch_create(int device, const mf_ic_request* items, int nitems, int nstreams, int flags, mf_batch** out);
 int mf_batch_destroy(mf_batch* b);
 /* new cosmology and seed of realizations [first, first+count) for the next
  * run (grid, box, order, lattice and precision stay); cosmology scalars are
@@ -55,6 +58,8 @@ int mf_batch_run(mf_batch* b, double* ms);
 int mf_batch_particles(mf_batch* b, int i, mf_particles* out);
 /* graph nodes, kernel launches per run, device bytes of all pipelines */
 int mf_batch_info(mf_batch* b, int* graph_nodes, long long* kernels, size_t* device_bytes);
+/* the autotuner's report (empty without MF_BATCH_AUTOTUNE) */
+const char* mf_batch_tuning(const mf_batch* b);
 /* message of the last failure on b; with b == NULL, of the last failed
  * mf_batch_create on the calling thread */
 const char* mf_batch_last_error(const mf_batch* b);

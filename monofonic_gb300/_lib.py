@@ -150,7 +150,12 @@ class mf_server_stats(C.Structure):
 
 
 SIGNATURES.update({
-    "mf_batch_create": (C.c_int, [C.c_int, C.POINTER(mf_ic_request), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "mf_batch_create": (C.c_int, [C.c_int, C.POINTER(mf_ic_request), C.c_int, C.c_int, C.c_int,
+                                  C.POINTER(C.c_void_p)]),
+    "mf_batch_tuning": (C.c_char_p, [C.c_void_p]),
+    "mf_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_size_t]),
+    "mf_autotune_reset": (C.c_int, []),
+    "mf_schedule_set": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "mf_batch_destroy": (C.c_int, [C.c_void_p]),
     "mf_batch_set_items": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(mf_cosmo_params),
                                      C.POINTER(C.c_uint64), C.c_int]),

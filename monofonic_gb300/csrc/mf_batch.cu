@@ -4,6 +4,7 @@
 // runs its realizations back to back, and the streams overlap.  The graph
 // is recorded once; a new seed or cosmology only changes the pipelines'
 // parameter blocks, which the graph copies to the device when it runs.
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -30,6 +31,7 @@ struct mf_batch {
   size_t device_bytes = 0;
   long long kernels = 0;
   std::string err;
+  std::string tuning;  // autotuner report
 };
 
 namespace {
@@ -123,7 +125,8 @@ extern "C" int mf_batch_destroy(mf_batch* b) {
   return MF_OK;
 }
 
-extern "C" int mf_batch_create(int device, const mf_ic_request* items, int nitems, int nstreams, mf_batch** out) {
+extern "C" int mf_batch_create(int device, const mf_ic_request* items, int nitems, int nstreams, int flags,
+                               mf_batch** out) {
   if (!out || !items || nitems <= 0) return MF_ERR_ARG;
   *out = nullptr;
   for (int i = 0; i < nitems; ++i) {
@@ -157,6 +160,22 @@ extern "C" int mf_batch_create(int device, const mf_ic_request* items, int nitem
   std::vector<mf_cosmo_scalars> sc;
   int rc = compute_scalars(items, nitems, sc, 0);
   if (rc != MF_OK) return fail(rc);
+  if (flags & MF_BATCH_AUTOTUNE) {  // schedules are read at launch, so tune before recording
+    std::vector<std::pair<int, int>> shapes;
+    for (int i = 0; i < nitems; ++i) {
+      const std::pair<int, int> k(items[i].ngrid, items[i].precision);
+      if (items[i].lpt_order > 1 && std::find(shapes.begin(), shapes.end(), k) == shapes.end()) shapes.push_back(k);
+    }
+    std::vector<char> rep(8192);
+    for (const auto& k : shapes) {
+      rc = mf_autotune(b->ctx[0], k.first, k.second, rep.data(), rep.size());
+      if (rc != MF_OK) {
+        b->err = std::string("autotune: ") + mf_last_error(b->ctx[0]);
+        return fail(rc);
+      }
+      b->tuning += rep.data();
+    }
+  }
   // largest realization first onto the least loaded lane
   std::vector<int> order(nitems);
   std::iota(order.begin(), order.end(), 0);
@@ -251,5 +270,7 @@ extern "C" int mf_batch_info(mf_batch* b, int* graph_nodes, long long* kernels, 
   if (device_bytes) *device_bytes = b->device_bytes;
   return MF_OK;
 }
+
+extern "C" const char* mf_batch_tuning(const mf_batch* b) { return b ? b->tuning.c_str() : ""; }
 
 extern "C" const char* mf_batch_last_error(const mf_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }

@@ -24,6 +24,8 @@
 #endif
 
 #include "mf_kernels.cuh"
+#include "mf_runtime.h"
+#include "mf_sched.h"
 
 namespace mf {
 
@@ -66,7 +68,7 @@ constexpr int pipe_ncol() {
 }
 
 template <typename T, int L, bool INV, class OP>
-cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s) {
+cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s, int kind) {
   if constexpr (OP::kPipe && MF_COL_PIPE) {
     constexpr int NC = pipe_ncol<T, L>();
     constexpr int TPL = LineFFT<T, L, INV>::TPL;
@@ -79,6 +81,8 @@ cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, c
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NC * TPL, smem);
     if (e != cudaSuccess) return e;
+    const PassSched sc = sched_get(kind, L, (int)sizeof(T));
+    if (sc.occ > 0 && sc.occ < per_sm) per_sm = sc.occ;
     if (per_sm < 1) per_sm = 1;
     const int ntc = (ncols + NC - 1) / NC;
     const int total = ntc * nslab * nz;
@@ -143,7 +147,8 @@ constexpr int tma_lines_per_batch() {
 // barriers when a line's threads fit in one warp.
 template <typename T, int H>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
-  {
+  const PassSched sc = sched_get(KK_CONV_Z, 2 * H, (int)sizeof(T));
+  if (sc.variant == 0) {
     // TMA path: radix-8-first plan with the padded (conflict-free) exchange layout
     constexpr int MAXR = MF_ZCONV_TMA_MAXR;
     constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
@@ -165,6 +170,7 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LPBT * TPL, smem);
       if (e != cudaSuccess) return e;
+      if (sc.occ > 0 && sc.occ < per_sm) per_sm = sc.occ;
       if (per_sm < 1) per_sm = 1;
       const int nbatch = a.nlines / LPBT;
       int grid = nsm * per_sm;
@@ -204,8 +210,8 @@ cudaError_t Launch<T>::colfft_plain(int L, bool inv, PlainStridedOp<T> op, int n
                                     const cplx<T>* tw, cudaStream_t s) {
 #define CASE(LL)                                                              \
   case LL:                                                                    \
-    return inv ? launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s)          \
-               : launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+    return inv ? launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s, KK_FFT_COL)   \
+               : launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_FFT_COL);
   switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
@@ -226,7 +232,7 @@ cudaError_t Launch<T>::z_c2r_plain(int H, PlainZOp<T> op, int nlines, int kin, c
 template <typename T>
 cudaError_t Launch<T>::assemble_xinv(int L, AssembleXInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                      cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s);
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s, KK_FFT_COL);
   switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
@@ -240,14 +246,14 @@ template cudaError_t Launch<MF_T>::z_c2r_plain(int, PlainZOp<MF_T>, int, int, co
 template <typename T>
 cudaError_t Launch<T>::conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
                                  const cplx<T>* tw, cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s);
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s, KK_CONV_XINV);
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
 template <typename T>
 cudaError_t Launch<T>::conv_xfwd(int L, ConvXFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                  cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_CONV_XFWD);
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
@@ -259,14 +265,14 @@ template cudaError_t Launch<MF_T>::conv_xfwd(int, ConvXFwdOp<MF_T>, int, int, co
 template <typename T>
 cudaError_t Launch<T>::conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,
                                  const cplx<T>* tw, cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s);
+#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s, KK_CONV_YINV);
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
 template <typename T>
 cudaError_t Launch<T>::conv_yfwd(int L, ConvYFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                  cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s);
+#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_CONV_YFWD);
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }

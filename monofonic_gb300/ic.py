@@ -242,3 +242,16 @@ def device_footprint(cfg: ICConfig, scalars) -> int:
     if rc != L.MF_OK:
         raise MFError(rc, "mf_ic_device_footprint")
     return b.value
+
+
+def autotune(ctx: Context, n: int, precision: str = "f32") -> str:
+    """mf_autotune: pick the fastest schedule of each convolution pass for grid
+    size n (process-wide, used by every later launch); returns the report"""
+    buf = C.create_string_buffer(8192)
+    prec = L.MF_PREC_F64 if precision == "f64" else L.MF_PREC_F32
+    _check(ctx.ptr, lib().mf_autotune(ctx.ptr, int(n), prec, buf, len(buf)))
+    return buf.value.decode()
+
+
+def autotune_reset():
+    lib().mf_autotune_reset()

@@ -69,11 +69,12 @@ def _particles_to_host(p: "L.mf_particles", req: Request):
 class Batch:
     """All realizations recorded into one CUDA graph over nstreams streams."""
 
-    def __init__(self, requests, nstreams: int = 8, device: int = 0):
+    def __init__(self, requests, nstreams: int = 8, device: int = 0, autotune: bool = False):
         self.requests = list(requests)
         arr = (L.mf_ic_request * len(self.requests))(*[r.to_c() for r in self.requests])
         p = C.c_void_p()
-        rc = lib().mf_batch_create(int(device), arr, len(self.requests), int(nstreams), C.byref(p))
+        rc = lib().mf_batch_create(int(device), arr, len(self.requests), int(nstreams), 1 if autotune else 0,
+                                   C.byref(p))
         if rc != L.MF_OK:
             msg = lib().mf_batch_last_error(None)
             raise MFError(rc, msg.decode() if msg else "mf_batch_create")
@@ -107,6 +108,12 @@ class Batch:
         p = L.mf_particles()
         self._check(lib().mf_batch_particles(self.ptr, int(i), C.byref(p)), "mf_batch_particles")
         return _particles_to_host(p, self.requests[i])
+
+    @property
+    def tuning(self) -> str:
+        """the autotuner's report (one line per pass kind and shape)"""
+        r = lib().mf_batch_tuning(self.ptr)
+        return r.decode() if r else ""
 
     def info(self):
         nodes, kern, nb = C.c_int(), C.c_longlong(), C.c_size_t()

@@ -114,7 +114,8 @@ def test_batch_equals_standalone_and_replays(ctx):
     reqs = _mixed_requests(rng, 7, [16, 32, 64])
     reqs[3].precision = "f64"
     reqs[5].lattice = "bcc"
-    b = Batch(reqs, nstreams=3)
+    b = Batch(reqs, nstreams=3, autotune=True)
+    assert "conv_z" in b.tuning
     info = b.info()
     assert info["graph_nodes"] > info["kernels"] > 0
     ms = b.run()
@@ -177,3 +178,54 @@ def test_server_admission_respects_budget(ctx):
     with pytest.raises(Exception):
         srv.submit(Request(ngrid=256, boxlen=512.0, lpt_order=3))  # larger than the budget
     srv.close()
+
+
+def test_autotune_keeps_parity(ctx):
+    """the autotuner changes schedules only: a convolution after tuning still
+    matches the oracle (FP64 1e-12), and the report names every pass"""
+    import monofonic_gb300 as mf
+    from monofonic_gb300 import ic
+    n, L = 32, 100.0
+    rep = ic.autotune(ctx, n, "f64")
+    for k in ("conv_xinv", "conv_yinv", "conv_z", "conv_yfwd", "conv_xfwd"):
+        assert f"{k} L=48 f64" in rep, rep
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((n, n, n))
+    g = mf.Grid_FFT(ctx, n, L, "f64")
+    g.set_real(x)
+    g.FourierTransformForward()
+    out = mf.Grid_FFT(ctx, n, L, "f64", "k")
+    cv = mf.OrszagConvolver(ctx, n, L, "f64")
+    cv.convolve_Hessians(g, (0, 1), g, (2, 2), mf.op.assign_to(out))
+    phi = O.r2c(x)
+    ref = O.orszag_conv2(O.hessian(phi, L, 0, 1), O.hessian(phi, L, 2, 2))
+    assert rel_l2(out.get_k(), ref) < 1e-12
+    ic.autotune_reset()
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_every_schedule_candidate_keeps_parity(ctx, prec, tol):
+    """each schedule the autotuner may pick, forced by hand: 1 or 2 CTAs per SM
+    for every pass, and the direct-load radix-4 z pass"""
+    import monofonic_gb300 as mf
+    from monofonic_gb300 import ic
+    lib = mf.lib()
+    pc = 0 if prec == "f64" else 1
+    L = 100.0
+    for n in (16, 32, 64):
+        M = 3 * n // 2
+        rng = np.random.default_rng(n)
+        x = rng.standard_normal((n, n, n))
+        phi = O.r2c(x)
+        ref = O.orszag_conv2(O.hessian(phi, L, 0, 0), O.sum_hessian(phi, L, (1, 1), (2, 2)))
+        g = mf.Grid_FFT(ctx, n, L, prec)
+        g.set_real(x)
+        g.FourierTransformForward()
+        cv = mf.OrszagConvolver(ctx, n, L, prec)
+        for occ, zvar in ((1, 0), (2, 0), (0, 1), (1, 1)):
+            for kind in range(5):
+                assert lib.mf_schedule_set(kind, M, pc, occ, zvar if kind == 2 else 0) == 0
+            out = mf.Grid_FFT(ctx, n, L, prec, "k")
+            cv.convolve_SumOfHessians(g, (0, 0), g, (1, 1), (2, 2), mf.op.assign_to(out))
+            assert rel_l2(out.get_k(), ref) < tol, (n, occ, zvar)
+        ic.autotune_reset()
