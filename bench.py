@@ -493,10 +493,20 @@ def run_mf(args):
         t = max_over_ranks(e0.elapsed_time(e1))
         ids_h = ids.array(np.uint64, (npart,))
         assert ids_h[1] == 2 and ids_h[n ** 3] == 1, "particle IDs wrong after e2e run"
+        # the box's raw device-to-host copy rate into page-locked memory, for context
+        probe = torch.empty(1 << 30, dtype=torch.uint8, device=torch.device("cuda", local))
+        best = 1e30
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mf.lib().mf_copy_to_host(pos.ptr, probe.data_ptr(), probe.numel())
+            best = min(best, time.perf_counter() - t0)
+        del probe
         e2e = {"value": world * npart * args.steps / (t / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": int(noise_h.nbytes),
                "d2h_bytes_per_step": int(gen32.pos_bytes + gen32.vel_bytes + gen32.id_bytes),
-               "ms_per_step": t / args.steps}
+               "ms_per_step": t / args.steps,
+               "box_d2h_GBps_pinned_1GiB": round((1 << 30) / best / 1e9, 1)}
         for b in (pin_noise, pos, vel, ids):
             b.close()
     gen32.close()

@@ -164,6 +164,12 @@ struct mf_ic {
   bool has_tk = false;      // amp + nk2 holds a tabulated T(k)
   ICDyn* dyn_h = nullptr;   // page-locked host copy, copied to dyn_d at the start of each run
   ICDyn* dyn_d = nullptr;
+  // host hand-off: the positions are copied on a second stream while the
+  // velocities are being assembled
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t ev_pos = nullptr, ev_copy = nullptr;
+  const mf_particles* early = nullptr;
+  bool pos_copied = false;
 };
 
 namespace {
@@ -412,6 +418,13 @@ int enqueue_impl(mf_ic* ic) {
       CK(cudaGetLastError());
     }
     if (timed) CK(cudaEventRecord(ic->ev[5 + pass], s));
+    if (pass == 0 && ic->early) {  // positions are final: start their copy to the host
+      CK(cudaEventRecord(ic->ev_pos, s));
+      CK(cudaStreamWaitEvent(ic->cstream, ic->ev_pos, 0));
+      CK(cudaMemcpyAsync(ic->early->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, ic->cstream));
+      CK(cudaEventRecord(ic->ev_copy, ic->cstream));
+      ic->pos_copied = true;
+    }
   }
   // ---- particle IDs (particle_generator.hh:212-253) ------------------------
   if (!fields) {
@@ -442,9 +455,10 @@ int handoff(mf_ic* ic, mf_particles* out) {
     out->npart = ic->npart;
     if (out->location == MF_LOC_HOST) {
       if (!out->pos || !out->vel || (!fields && !out->ids)) return set_err(c, MF_ERR_ARG, "mf_ic_run: null host buffer");
-      CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
+      if (!ic->pos_copied) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, s));
       if (!fields) CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, s));
+      if (ic->pos_copied) CK(cudaStreamWaitEvent(s, ic->ev_copy, 0));  // the run ends after both copies
     } else {
       out->pos = ic->dpos;
       out->vel = ic->dvel;
@@ -513,6 +527,12 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
     if (e) cudaEventDestroy(e);
   cudaFree(ic->dyn_d);
   cudaFreeHost(ic->dyn_h);
+  if (ic->cstream) {
+    cudaStreamSynchronize(ic->cstream);
+    cudaStreamDestroy(ic->cstream);
+  }
+  if (ic->ev_pos) cudaEventDestroy(ic->ev_pos);
+  if (ic->ev_copy) cudaEventDestroy(ic->ev_copy);
   --c->children;
   delete ic;
   return MF_OK;
@@ -692,10 +712,23 @@ extern "C" int mf_ic_enqueue(mf_ic* ic) {
 extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
   if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
+  ic->early = nullptr;
+  ic->pos_copied = false;
+  if (out && out->location == MF_LOC_HOST && out->pos && out->vel) {
+    cudaError_t e = cudaSuccess;
+    if (!ic->cstream) e = cudaStreamCreateWithFlags(&ic->cstream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !ic->ev_pos) e = cudaEventCreateWithFlags(&ic->ev_pos, cudaEventDisableTiming);
+    if (e == cudaSuccess && !ic->ev_copy) e = cudaEventCreateWithFlags(&ic->ev_copy, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_err(ic->ctx, e, "mf_ic_run: copy stream");
+    ic->early = out;
+  }
   int rc = mf_ic_enqueue(ic);
   if (rc == MF_OK) rc = handoff(ic, out);
   if (rc == MF_OK) rc = check_device_error(ic->ctx);
   else cudaStreamSynchronize(ic->ctx->stream);
+  if (ic->cstream) cudaStreamSynchronize(ic->cstream);
+  ic->early = nullptr;
+  ic->pos_copied = false;
   return rc;
 }
 
