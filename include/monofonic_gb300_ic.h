@@ -85,6 +85,10 @@ typedef struct {
   int pos64;              /* output_plugin::has_64bit_reals                 */
   int id64;               /* output_plugin::has_64bit_ids                   */
   int plt_ngrid;          /* PLT mesh size (lattice_gradient ngridself); 0: 64 */
+  int per_term_conv;      /* 0: Orszag source terms through shared padded
+                             real fields (each operand transformed once);
+                             1: one convolution per term as the reference
+                             orders them (less device memory) */
 } mf_ic_params;
 
 /* Particle container (include/particle_container.hh:29-139): positions and

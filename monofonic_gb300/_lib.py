@@ -87,7 +87,8 @@ class mf_ic_params(C.Structure):
                 ("lattice", C.c_int), ("precision", C.c_int), ("convolver", C.c_int), ("fixing", C.c_int),
                 ("inversion", C.c_int), ("plt", C.c_int), ("cosmo", mf_cosmo_scalars),
                 ("tk_table", C.c_void_p), ("lunit", C.c_double), ("vunit", C.c_double), ("out_kind", C.c_int),
-                ("pos64", C.c_int), ("id64", C.c_int), ("plt_ngrid", C.c_int)]
+                ("pos64", C.c_int), ("id64", C.c_int), ("plt_ngrid", C.c_int),
+                ("per_term_conv", C.c_int)]
 
 
 class mf_particles(C.Structure):

@@ -3,6 +3,7 @@
 // Orszag convolver -> displacement/velocity assembly -> lattice positions,
 // velocities and particle IDs.
 #include <cmath>
+#include <initializer_list>
 #include <cstring>
 #include <new>
 #include <string>
@@ -170,9 +171,20 @@ struct mf_ic {
   cudaEvent_t ev_pos = nullptr, ev_copy = nullptr;
   const mf_particles* early = nullptr;
   bool pos_copied = false;
+  // shared-source convolutions: padded real fields and three work buffers
+  bool shared = false;
+  void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs
+  void* w3 = nullptr;   // three work buffers [M][M][N/2+1] complex
+  mf_grid* qx = nullptr;  // fifth N-grid buffer of the phi(3) pair products
 };
 
 namespace {
+
+// the Orszag source terms through shared padded real fields (default), or
+// one convolution per term (per_term_conv, or the aliased convolver)
+bool uses_shared_sources(const mf_ic_params* p) {
+  return p->lpt_order > 1 && p->convolver == MF_CONV_ORSZAG && !p->per_term_conv;
+}
 
 int check_params(const mf_ic_params* p) {
   if (!p) return MF_ERR_ARG;
@@ -219,6 +231,180 @@ void fill_dyn(mf_ic* ic) {
   const double g3c = (p.lpt_order > 2) ? 1.0 / 7.0 * D * D * D : 0.0;
   d.w[0][0] = g1; d.w[0][1] = g2; d.w[0][2] = g3; d.w[0][3] = g3c;
   d.w[1][0] = vf * g1; d.w[1][1] = 2 * vf * g2; d.w[1][2] = 3 * vf * g3; d.w[1][3] = 3 * vf * g3c;
+}
+
+// phi(2), phi(3) and A(3) with shared padded real fields (ic_generator.cc:471-545).
+// Every Orszag convolution of the reference multiplies two padded operands in
+// real space, transforms the product back and unpads it into the target
+// through a linear op::.  By linearity of the r2c and of the unpad, the sum
+// of the target's convolutions equals one r2c and unpad of the sum of the
+// real-space products, so each distinct operand (the six Hessians of phi,
+// the six of phi(2), the five truncated pair products of convolve3's first
+// stage) is transformed to padded real space once, and each target is one
+// product sum, one r2c and one unpad.  convolve3 keeps its intermediate
+// truncation: the pair product is unpadded into an N-grid (Nyquist zeroed)
+// and transformed again before the third factor multiplies it.
+template <typename T>
+int shared_sources(mf_ic* ic, bool timed) {
+  mf_ctx* c = ic->ctx;
+  cudaStream_t s = c->stream;
+  const mf_ic_params& p = ic->p;
+  const int N = p.ngrid, M = 3 * N / 2, Kz = N / 2 + 1, H = M / 2;
+  const ConvGeom g{N, M, Kz, true};
+  const T kfac = T(2.0 * M_PI / p.boxlen);
+  const double M3 = (double)M * M * M, N3 = (double)N * N * N;
+  const T scale_in = T(std::pow(1.5, 1.5) / std::sqrt(M3));
+  const T scale_out = T(1.0 / std::sqrt(M3) / (std::sqrt(M3) / std::sqrt(N3)));
+  const cplx<T>* twM = c->tw.get<T>(M, s);
+  const cplx<T>* twH = c->tw.get<T>(H, s);
+  if (!twM || !twH) return set_err(c, MF_ERR_OOM, "twiddles");
+  const size_t per = (size_t)M * M * Kz;
+  cplx<T>* W[3] = {(cplx<T>*)ic->w3, (cplx<T>*)ic->w3 + per, (cplx<T>*)ic->w3 + 2 * per};
+  const size_t rl = (size_t)M * M * H;
+  auto R = [&](int i) { return (cplx<T>*)ic->rf + (size_t)i * rl; };
+  cudaError_t e;
+#define CK(x)                                            \
+  do {                                                   \
+    e = (x);                                             \
+    if (e != cudaSuccess) return cuda_err(c, e, #x);     \
+  } while (0)
+
+  // padded c2r of up to three operands into real fields dst[k]
+  auto c2r = [&](int nop, const Operand<T>* ops, const int* dst) -> cudaError_t {
+    ConvXInvOp<T> xo{};
+    for (int k = 0; k < nop; ++k) { xo.opnd[k] = ops[k]; xo.dst[k] = W[k]; }
+    xo.g = g;
+    xo.kfac = kfac;
+    xo.scale = scale_in;
+    cudaError_t e2;
+    {
+      LaunchScope ls(c, KK_CONV_XINV);
+      if ((e2 = Launch<T>::conv_xinv(M, xo, N, Kz, nop, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvYInvOp<T> yo{};
+    for (int k = 0; k < nop; ++k) { yo.src[k] = W[k]; yo.dst[k] = W[k]; }
+    yo.g = g;
+    {
+      LaunchScope ls(c, KK_CONV_YINV);
+      if ((e2 = Launch<T>::conv_yinv(M, yo, M, Kz, nop, twM, s)) != cudaSuccess) return e2;
+    }
+    for (int k = 0; k < nop; ++k) {
+      LaunchScope ls(c, KK_CONV_Z);
+      if ((e2 = Launch<T>::z_c2r_pad(H, PadC2RZOp<T>{W[k], Kz, R(dst[k]), H}, M * M, Kz, twH, twM, s)) != cudaSuccess)
+        return e2;
+    }
+    return cudaSuccess;
+  };
+  struct Term { int a, b; double w; };
+  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2)
+  auto prod = [&](std::initializer_list<Term> terms, cplx<T>* target, int op, int invlap) -> cudaError_t {
+    ProdR2CZOp<T> po{};
+    int t = 0;
+    for (const Term& tm : terms) {
+      po.fa[t] = R(tm.a);
+      po.fb[t] = R(tm.b);
+      po.w[t] = T(tm.w);
+      ++t;
+    }
+    po.nterm = t;
+    po.H = H;
+    po.dst = W[0];
+    po.dst_stride = Kz;
+    cudaError_t e2;
+    {
+      LaunchScope ls(c, KK_CONV_Z);
+      if ((e2 = Launch<T>::z_r2c_prod(H, po, M * M, Kz, twH, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvYFwdOp<T> yf{W[0], W[0], g};
+    {
+      LaunchScope ls(c, KK_CONV_YFWD);
+      if ((e2 = Launch<T>::conv_yfwd(M, yf, M, Kz, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvXFwdOp<T> xf{};
+    xf.src = W[0];
+    xf.target = target;
+    xf.g = g;
+    xf.scale = scale_out;
+    xf.out_op = op;
+    xf.x = T(1);
+    xf.post_invlap = invlap;
+    xf.kfac = kfac;
+    LaunchScope ls(c, KK_CONV_XFWD);
+    return Launch<T>::conv_xfwd(M, xf, N, Kz, twM, s);
+  };
+  // Hessian field index: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2)
+  auto hx = [](int a, int b) {
+    if (a > b) { const int t = a; a = b; b = t; }
+    return (a == b) ? a : (a == 0 ? (b == 1 ? 3 : 4) : 5);
+  };
+  const int HD[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  auto hessians = [&](int fi, int base) -> cudaError_t {
+    for (int half = 0; half < 2; ++half) {
+      Operand<T> ops[3];
+      int dst[3];
+      for (int k = 0; k < 3; ++k) {
+        ops[k] = Operand<T>{};
+        ops[k].f = (const cplx<T>*)ic->f[fi]->d;
+        ops[k].kind = OPND_HESS;
+        ops[k].d[0] = HD[3 * half + k][0];
+        ops[k].d[1] = HD[3 * half + k][1];
+        dst[k] = base + 3 * half + k;
+      }
+      cudaError_t e2 = c2r(3, ops, dst);
+      if (e2 != cudaSuccess) return e2;
+    }
+    return cudaSuccess;
+  };
+
+  // ---- phi(2) (ic_generator.cc:471-488) ----------------------------------
+  CK(hessians(0, 0));
+  CK(prod({{0, 1, 1.0}, {0, 2, 1.0}, {1, 2, 1.0}, {3, 3, -1.0}, {4, 4, -1.0}, {5, 5, -1.0}},
+          (cplx<T>*)ic->f[1]->d, OUT_ASSIGN, 1));
+  ic->f[1]->space = MF_SPACE_K;
+  if (timed) CK(cudaEventRecord(ic->ev[2], s));
+  if (p.lpt_order > 2) {
+    // ---- phi(3) (ic_generator.cc:511-528) --------------------------------
+    CK(hessians(1, 6));
+    // convolve3 first stages: truncated pair products phi,00 phi,11 / phi,01 phi,02 /
+    // phi,12^2 / phi,02^2 / phi,01^2, then their padded c2r
+    mf_grid* qg[5] = {ic->tmp[0], ic->tmp[1], ic->tmp[2], ic->wn, ic->qx};
+    const int pa[5][2] = {{0, 1}, {3, 4}, {5, 5}, {4, 4}, {3, 3}};
+    for (int k = 0; k < 5; ++k) CK(prod({{pa[k][0], pa[k][1], 1.0}}, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
+    {
+      Operand<T> ops[3];
+      int dst[3];
+      for (int b0 = 0; b0 < 5; b0 += 3) {
+        const int nb = (5 - b0 < 3) ? 5 - b0 : 3;
+        for (int k = 0; k < nb; ++k) {
+          ops[k] = Operand<T>{};
+          ops[k].f = (const cplx<T>*)qg[b0 + k]->d;
+          ops[k].kind = OPND_PLAIN;
+          dst[k] = 12 + b0 + k;
+        }
+        CK(c2r(nb, ops, dst));
+      }
+    }
+    const double a5 = -5.0 / 7.0, a10 = 10.0 / 7.0;
+    CK(prod({{12, 2, 1.0}, {13, 5, 2.0}, {14, 0, -1.0}, {15, 1, -1.0}, {16, 2, -1.0},
+             {0, 7, a5}, {0, 8, a5}, {1, 8, a5}, {1, 6, a5}, {2, 6, a5}, {2, 7, a5},
+             {3, 9, a10}, {4, 10, a10}, {5, 11, a10}},
+            (cplx<T>*)ic->f[2]->d, OUT_ASSIGN, 1));
+    ic->f[2]->space = MF_SPACE_K;
+    if (timed) CK(cudaEventRecord(ic->ev[3], s));
+    // ---- A(3) (ic_generator.cc:534-545) ---------------------------------
+    for (int d = 0; d < 3; ++d) {
+      const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
+      CK(prod({{6 + hx(d, dp), hx(d, dpp), 1.0}, {6 + hx(d, dpp), hx(d, dp), -1.0},
+               {hx(dp, dpp), 6 + hx(dp, dp), 1.0}, {hx(dp, dpp), 6 + hx(dpp, dpp), -1.0},
+               {6 + hx(dp, dpp), hx(dp, dp), -1.0}, {6 + hx(dp, dpp), hx(dpp, dpp), 1.0}},
+              (cplx<T>*)ic->f[3 + d]->d, OUT_ASSIGN, 1));
+      ic->f[3 + d]->space = MF_SPACE_K;
+    }
+  } else if (timed) {
+    CK(cudaEventRecord(ic->ev[3], s));
+  }
+#undef CK
+  return MF_OK;
 }
 
 // the whole pipeline on the context's stream, without host synchronisation
@@ -298,8 +484,12 @@ int enqueue_impl(mf_ic* ic) {
     return conv_run<T>(ic->conv, o2, 2, (cplx<T>*)ic->f[tgt]->d, op, T(x), 0);
   };
 
+  if (ic->shared) {
+    const int rc = shared_sources<T>(ic, timed);
+    if (rc != MF_OK) return rc;
+  }
   // ---- phi(2) (ic_generator.cc:471-488) ----------------------------------
-  if (p.lpt_order > 1) {
+  if (p.lpt_order > 1 && !ic->shared) {
     CK(conv2(H(0, 0, 0), S(0, 1, 1, 2, 2, false), 1, OUT_ASSIGN, 1, 0));
     CK(conv2(H(0, 1, 1), H(0, 2, 2), 1, OUT_ADD, 1, 0));
     CK(conv2(H(0, 0, 1), H(0, 0, 1), 1, OUT_SUB, 1, 0));
@@ -307,9 +497,9 @@ int enqueue_impl(mf_ic* ic) {
     CK(conv2(H(0, 1, 2), H(0, 1, 2), 1, OUT_SUB, 1, 1));
     ic->f[1]->space = MF_SPACE_K;
   }
-  if (timed) CK(cudaEventRecord(ic->ev[2], s));
+  if (timed && !ic->shared) CK(cudaEventRecord(ic->ev[2], s));
   // ---- phi(3) (ic_generator.cc:511-528) ----------------------------------
-  if (p.lpt_order > 2) {
+  if (p.lpt_order > 2 && !ic->shared) {
     CK(conv3(H(0, 0, 0), H(0, 1, 1), H(0, 2, 2), 2, OUT_ASSIGN, 1));
     CK(conv3(H(0, 0, 1), H(0, 0, 2), H(0, 1, 2), 2, OUT_AXPY, 2.0));
     CK(conv3(H(0, 1, 2), H(0, 1, 2), H(0, 0, 0), 2, OUT_SUB, 1));
@@ -323,9 +513,9 @@ int enqueue_impl(mf_ic* ic) {
     CK(conv2(H(0, 1, 2), H(1, 1, 2), 2, OUT_AXPY, +10.0 / 7.0, 1));
     ic->f[2]->space = MF_SPACE_K;
   }
-  if (timed) CK(cudaEventRecord(ic->ev[3], s));
+  if (timed && !ic->shared) CK(cudaEventRecord(ic->ev[3], s));
   // ---- A(3) (ic_generator.cc:534-545) -----------------------------------
-  if (p.lpt_order > 2) {
+  if (p.lpt_order > 2 && !ic->shared) {
     for (int d = 0; d < 3; ++d) {
       const int dp = (d + 1) % 3, dpp = (d + 2) % 3, tg = 3 + d;
       CK(conv2(H(1, d, dp), H(0, d, dpp), tg, OUT_ASSIGN, 1, 0));
@@ -495,8 +685,13 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   size_t conv = 0;
   if (p->lpt_order > 1) {
     const size_t M = (p->convolver == MF_CONV_ORSZAG) ? 3 * n / 2 : n;
-    const int nbuf = (p->convolver == MF_CONV_ORSZAG) ? 2 : 3;
-    conv = (size_t)nbuf * M * M * (n / 2 + 1) * 2 * ps + (p->convolver == MF_CONV_ORSZAG ? grid : 0);
+    if (uses_shared_sources(p)) {
+      const size_t nreal = (p->lpt_order > 2) ? 17 : 6;
+      conv = 3 * M * M * (n / 2 + 1) * 2 * ps + nreal * M * M * M * ps + (p->lpt_order > 2 ? grid : 0);
+    } else {
+      const int nbuf = (p->convolver == MF_CONV_ORSZAG) ? 2 : 3;
+      conv = (size_t)nbuf * M * M * (n / 2 + 1) * 2 * ps + (p->convolver == MF_CONV_ORSZAG ? grid : 0);
+    }
   }
   int64_t np; size_t pb, vb, ib;
   output_sizes(p, &np, &pb, &vb, &ib);
@@ -519,6 +714,9 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->qtab);
   cudaFree(ic->plt);
   if (ic->conv) mf_conv_destroy(ic->conv);
+  if (ic->qx) mf_grid_destroy(ic->qx);
+  cudaFree(ic->rf);
+  cudaFree(ic->w3);
   cudaFree(ic->amp);
   cudaFree(ic->dpos);
   cudaFree(ic->dvel);
@@ -610,8 +808,17 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     if (e3 == cudaSuccess) e3 = cudaMemcpy(ic->plt, h.data(), h.size(), cudaMemcpyHostToDevice);
     if (e3 != cudaSuccess) return fail(cuda_err(c, e3, "mf_ic_create: PLT tables"));
   }
-  if (p->lpt_order > 1)
+  if (uses_shared_sources(p)) {
+    ic->shared = true;
+    const size_t M = 3 * (size_t)n / 2, cs = (p->precision == MF_PREC_F32) ? sizeof(float2) : sizeof(double2);
+    const size_t nreal = (p->lpt_order > 2) ? 17 : 6;
+    cudaError_t e4 = cudaMalloc(&ic->rf, nreal * M * M * (M / 2) * cs);
+    if (e4 == cudaSuccess) e4 = cudaMalloc(&ic->w3, 3 * M * M * (n / 2 + 1) * cs);
+    if (e4 != cudaSuccess) return fail(cuda_err(c, e4, "mf_ic_create: shared-source buffers"));
+    if (p->lpt_order > 2 && (rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->qx))) return fail(rc);
+  } else if (p->lpt_order > 1) {
     if ((rc = mf_conv_create(c, n, p->boxlen, p->precision, p->convolver, &ic->conv))) return fail(rc);
+  }
   ic->nk2 = 3 * (n / 2) * (n / 2) + 1;
   cudaError_t e = cudaMalloc(&ic->amp, sizeof(double) * 2 * ic->nk2);
   if (e != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: amplitude table"));

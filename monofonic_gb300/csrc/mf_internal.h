@@ -69,6 +69,11 @@ struct Launch {
                                  const cplx<T>* twM, cudaStream_t s);
   static cudaError_t z_conv(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                             cudaStream_t s);
+  // z passes of the shared-source convolutions (padded lengths)
+  static cudaError_t z_c2r_pad(int H, PadC2RZOp<T> op, int nlines, int kin, const cplx<T>* twH,
+                               const cplx<T>* twM, cudaStream_t s);
+  static cudaError_t z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
+                                const cplx<T>* twM, cudaStream_t s);
 };
 
 }  // namespace mf

@@ -84,6 +84,7 @@ class ICConfig:
     pos64: bool = True
     id64: bool = True
     plt_ngrid: int = 0
+    per_term_conv: bool = False
 
     def to_c(self, scalars, tk_table=None):
         p = L.mf_ic_params()
@@ -105,6 +106,7 @@ class ICConfig:
         p.pos64 = int(self.pos64)
         p.id64 = int(self.id64)
         p.plt_ngrid = int(self.plt_ngrid)
+        p.per_term_conv = int(self.per_term_conv)
         return p
 
 

@@ -136,3 +136,27 @@ def test_rejects_bad_params(ctx):
     with pytest.raises(MFError) as e:
         g.run()
     assert "MF_ERR_STATE" in str(e.value)
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_shared_sources_equal_per_term_convolutions(ctx, prec, tol):
+    """the shared padded real fields (default) and one Orszag convolution per
+    source term (the reference's order) give the same potentials and particles"""
+    from monofonic_gb300 import ic
+    n, L, z = 32, 80.0, 24.0
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, 8080)
+    out = []
+    for per_term in (False, True):
+        cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=3, lattice="bcc", precision=prec,
+                          lunit=L, vunit=L, per_term_conv=per_term)
+        g, parts = run_gpu(ctx, cfg, sc, noise)
+        out.append(([g.potential(w).astype(np.complex128) for w in range(6)], parts))
+        g.close()
+    (pa, (xa, va, ia)), (pb, (xb, vb, ib)) = out
+    for w in range(6):
+        assert rel_l2(pa[w], pb[w]) < tol, w
+    q = lattice_q(n, 1, L)
+    assert rel_l2(xa - q, xb - q) < tol
+    assert rel_l2(va, vb) < tol
+    assert np.array_equal(ia, ib)
