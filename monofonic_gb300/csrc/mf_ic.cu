@@ -173,7 +173,7 @@ struct mf_ic {
   bool pos_copied = false;
   // shared-source convolutions: padded real fields and three work buffers
   bool shared = false;
-  void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs
+  void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last: product sums)
   void* w3 = nullptr;   // three work buffers [M][M][N/2+1] complex
   mf_grid* qx = nullptr;  // fifth N-grid buffer of the phi(3) pair products
 };
@@ -289,31 +289,63 @@ int shared_sources(mf_ic* ic, bool timed) {
       if ((e2 = Launch<T>::conv_yinv(M, yo, M, Kz, nop, twM, s)) != cudaSuccess) return e2;
     }
     for (int k = 0; k < nop; ++k) {
+      ZConvArgs<T> za{};
+      za.in[0] = W[k];
+      za.out = R(dst[k]);
+      za.nop = 1;
+      za.kin = Kz;
+      za.kout = H;
+      za.in_stride = Kz;
+      za.out_stride = H;
+      za.nlines = M * M;
+      za.out_scale = T(1);
+      za.err = c->d_err;
       LaunchScope ls(c, KK_CONV_Z);
-      if ((e2 = Launch<T>::z_c2r_pad(H, PadC2RZOp<T>{W[k], Kz, R(dst[k]), H}, M * M, Kz, twH, twM, s)) != cudaSuccess)
-        return e2;
+      if ((e2 = Launch<T>::z_c2r_tma(H, za, twH, twM, s)) != cudaSuccess) return e2;
     }
     return cudaSuccess;
   };
   struct Term { int a, b; double w; };
-  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2)
+  const int pidx_field = (p.lpt_order > 2) ? 17 : 6;  // scratch field of the product sums
+  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2).
+  // With one or two distinct fields the product is formed inside the z pass;
+  // with more, a streaming pointwise kernel forms it first (every field read
+  // once at full bandwidth) and the z pass transforms the single sum.
   auto prod = [&](std::initializer_list<Term> terms, cplx<T>* target, int op, int invlap) -> cudaError_t {
     ProdR2CZOp<T> po{};
-    int t = 0;
+    ProdSum<T> ps{};
+    int t = 0, distinct[2 * kMaxProdTerms], nd = 0;
     for (const Term& tm : terms) {
       po.fa[t] = R(tm.a);
       po.fb[t] = R(tm.b);
       po.w[t] = T(tm.w);
+      ps.fa[t] = (const T*)R(tm.a);
+      ps.fb[t] = (const T*)R(tm.b);
+      ps.w[t] = T(tm.w);
+      for (int f : {tm.a, tm.b}) {
+        bool seen = false;
+        for (int q = 0; q < nd; ++q) seen |= distinct[q] == f;
+        if (!seen) distinct[nd++] = f;
+      }
       ++t;
     }
-    po.nterm = t;
+    po.nterm = ps.nterm = t;
     po.H = H;
     po.dst = W[0];
     po.dst_stride = Kz;
     cudaError_t e2;
-    {
+    if (nd <= 2) {
       LaunchScope ls(c, KK_CONV_Z);
       if ((e2 = Launch<T>::z_r2c_prod(H, po, M * M, Kz, twH, twM, s)) != cudaSuccess) return e2;
+    } else {
+      {
+        LaunchScope ls(c, KK_POINTWISE);
+        if ((e2 = pw_prodsum<T>((T*)R(pidx_field), 2 * rl, ps, s)) != cudaSuccess) return e2;
+      }
+      LaunchScope ls(c, KK_CONV_Z);
+      if ((e2 = Launch<T>::z_r2c_pad(H, PadR2CZOp<T>{R(pidx_field), H, W[0], Kz}, M * M, Kz, twH, twM, s)) !=
+          cudaSuccess)
+        return e2;
     }
     ConvYFwdOp<T> yf{W[0], W[0], g};
     {
@@ -686,7 +718,7 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   if (p->lpt_order > 1) {
     const size_t M = (p->convolver == MF_CONV_ORSZAG) ? 3 * n / 2 : n;
     if (uses_shared_sources(p)) {
-      const size_t nreal = (p->lpt_order > 2) ? 17 : 6;
+      const size_t nreal = (p->lpt_order > 2) ? 18 : 7;
       conv = 3 * M * M * (n / 2 + 1) * 2 * ps + nreal * M * M * M * ps + (p->lpt_order > 2 ? grid : 0);
     } else {
       const int nbuf = (p->convolver == MF_CONV_ORSZAG) ? 2 : 3;
@@ -811,7 +843,7 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   if (uses_shared_sources(p)) {
     ic->shared = true;
     const size_t M = 3 * (size_t)n / 2, cs = (p->precision == MF_PREC_F32) ? sizeof(float2) : sizeof(double2);
-    const size_t nreal = (p->lpt_order > 2) ? 17 : 6;
+    const size_t nreal = (p->lpt_order > 2) ? 18 : 7;  // operands + the product-sum scratch field
     cudaError_t e4 = cudaMalloc(&ic->rf, nreal * M * M * (M / 2) * cs);
     if (e4 == cudaSuccess) e4 = cudaMalloc(&ic->w3, 3 * M * M * (n / 2 + 1) * cs);
     if (e4 != cudaSuccess) return fail(cuda_err(c, e4, "mf_ic_create: shared-source buffers"));

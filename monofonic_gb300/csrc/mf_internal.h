@@ -74,6 +74,11 @@ struct Launch {
                                const cplx<T>* twM, cudaStream_t s);
   static cudaError_t z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
                                 const cplx<T>* twM, cudaStream_t s);
+  static cudaError_t z_r2c_pad(int H, PadR2CZOp<T> op, int nlines, int kout, const cplx<T>* twH,
+                               const cplx<T>* twM, cudaStream_t s);
+  // z_c2r_pad through the TMA-pipelined z pass (a.nop = 1, a.out = real field)
+  static cudaError_t z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
+                               cudaStream_t s);
 };
 
 }  // namespace mf

@@ -324,7 +324,9 @@ __device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin,
   return mkc<T>(Ev.x - Ov.y, Ev.y + Ov.x);
 }
 
-template <typename T, int H, int MAXR, int LPB, class SYNC>
+// C2R_ONLY: the inverse transform of one operand only, its real line
+// (M reals as H packed pairs) stored to out[line * out_stride + m]
+template <typename T, int H, int MAXR, int LPB, class SYNC, bool C2R_ONLY = false>
 __global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR, true>::TPL)
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
   using FI = LineFFT<T, H, true, MAXR, true>;
@@ -390,24 +392,30 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
         for (int s = 0; s < E; ++s) { prod[s].x *= v[s].x; prod[s].y *= v[s].y; }
       }
     }
-    sync();
+    if constexpr (C2R_ONLY) {
+      C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
 #pragma unroll
-    for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
-    sync();
+      for (int s = 0; s < E; ++s) dst[FI::out_index(t, s)] = prod[s];
+    } else {
+      sync();
 #pragma unroll
-    for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
-    FF::run(v, t, sm, 1, twH, sync);
-    sync();
+      for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
+      sync();
 #pragma unroll
-    for (int s = 0; s < E; ++s) sm[pidx<true>(FF::out_index(t, s))] = v[s];
-    sync();
-    C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
-    for (int k = t; k < a.kout; k += TPL) {
-      const C zk = sm[pidx<true>(k % H)];
-      const C zc = cconj(sm[pidx<true>((H - k) % H)]);
-      const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
-      const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
-      dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);
+      for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
+      FF::run(v, t, sm, 1, twH, sync);
+      sync();
+#pragma unroll
+      for (int s = 0; s < E; ++s) sm[pidx<true>(FF::out_index(t, s))] = v[s];
+      sync();
+      C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
+      for (int k = t; k < a.kout; k += TPL) {
+        const C zk = sm[pidx<true>(k % H)];
+        const C zc = cconj(sm[pidx<true>((H - k) % H)]);
+        const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
+        const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
+        dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);
+      }
     }
     __syncthreads();  // stage[st] fully consumed before it is refilled
   }

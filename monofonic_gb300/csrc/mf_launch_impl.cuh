@@ -145,10 +145,12 @@ constexpr int tma_lines_per_batch() {
 // lines is one 16-byte aligned contiguous block per operand, otherwise the
 // direct-load kernel.  Radix-4 plan (fewer registers per thread); warp
 // barriers when a line's threads fit in one warp.
-template <typename T, int H>
+// C2R_ONLY: the shared-source inverse transform of one operand into a real
+// padded field (fallback: the direct-load plain c2r kernel)
+template <typename T, int H, bool C2R_ONLY = false>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
   const PassSched sc = sched_get(KK_CONV_Z, 2 * H, (int)sizeof(T));
-  if (sc.variant == 0) {
+  if (sc.variant == 0 || C2R_ONLY) {
     // TMA path: radix-8-first plan with the padded (conflict-free) exchange layout
     constexpr int MAXR = MF_ZCONV_TMA_MAXR;
     constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
@@ -160,7 +162,7 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
                         (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
     if (tma_ok) {
-      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC>;
+      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, C2R_ONLY>;
       const size_t smem =
           128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * padded_len(H, true)) * sizeof(cplx<T>);
       cudaError_t e = set_smem(kern, smem);
@@ -178,6 +180,10 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
       kern<<<grid, LPBT * TPL, smem, s>>>(a, twH, twM);
       return cudaGetLastError();
     }
+  }
+  if constexpr (C2R_ONLY) {
+    return launch_zc2r<T, H>(PadC2RZOp<T>{a.in[0], a.in_stride, a.out, (int)a.out_stride}, a.nlines, a.kin, twH,
+                             twM, s);
   }
   // direct-load fallback: radix-4 plan, unpadded
   constexpr int MAXR = 4;
@@ -297,12 +303,28 @@ cudaError_t Launch<T>::z_c2r_pad(int H, PadC2RZOp<T> op, int nlines, int kin, co
 #undef CASE
 }
 template <typename T>
+cudaError_t Launch<T>::z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
+                                 cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zconv<T, HH, true>(a, twH, twM, s);
+  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::z_c2r_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
+template <typename T>
 cudaError_t Launch<T>::z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
                                   const cplx<T>* twM, cudaStream_t s) {
 #define CASE(HH) case HH: return launch_zr2c<T, HH>(op, nlines, kout, twH, twM, s);
   switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T>
+cudaError_t Launch<T>::z_r2c_pad(int H, PadR2CZOp<T> op, int nlines, int kout, const cplx<T>* twH,
+                                 const cplx<T>* twM, cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zr2c<T, HH>(op, nlines, kout, twH, twM, s);
+  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::z_r2c_pad(int, PadR2CZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_c2r_pad(int, PadC2RZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_r2c_prod(int, const ProdR2CZOp<MF_T>&, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 #endif

@@ -464,6 +464,27 @@ struct ProdR2CZOp {
   __device__ __forceinline__ void store(int line, int k, C v) const { dst[line * dst_stride + k] = v; }
 };
 
+// z pass r2c of one real padded field, keeping kz < kout
+template <typename T>
+struct PadR2CZOp {
+  using C = cplx<T>;
+  const C* src;
+  int H;
+  C* dst;
+  long long dst_stride;  // Kz
+  __device__ __forceinline__ C load_pair(int line, int m) const { return src[(long long)line * H + m]; }
+  __device__ __forceinline__ void store(int line, int k, C v) const { dst[line * dst_stride + k] = v; }
+};
+
+// pointwise sum of products of real fields, out = sum_t w_t a_t b_t
+template <typename T>
+struct ProdSum {
+  const T* fa[kMaxProdTerms];
+  const T* fb[kMaxProdTerms];
+  T w[kMaxProdTerms];
+  int nterm;
+};
+
 // arguments of the fused Orszag z pass (mf_kernels.cuh, k_zconv)
 template <typename T>
 struct ZConvArgs {
