@@ -113,7 +113,9 @@ typedef struct mf_ic mf_ic;
 /* allocate the pipeline's device state for a parameter set */
 int mf_ic_create(mf_ctx* ctx, const mf_ic_params* p, mf_ic** out);
 int mf_ic_destroy(mf_ic* ic);
-/* upload the real-space white noise (n^3 float64, host or device pointer) */
+/* upload the real-space white noise (n^3 float64, host or device pointer);
+ * an FP32 pipeline keeps an n^3-double staging buffer from its first host
+ * upload on */
 int mf_ic_set_noise(mf_ic* ic, const double* noise, int location);
 /* generate the white noise on the device from a seed at the start of every
  * run (the generator of mf_white_noise_host; no host field, no upload) */

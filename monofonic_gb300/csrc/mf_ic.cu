@@ -121,6 +121,26 @@ __global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P
   }
 }
 
+// PLT gradient and growth-rate correction of every N-grid mode, tabulated
+// once per pipeline (they depend on the lattice, N and the PLT mesh only):
+// out[4 idx + {0,1,2,3}] = g_x, g_y, g_z, vfac_corr
+template <typename T>
+__global__ void k_plt_grad_table(T* __restrict__ out, int n, PLTDev<T> P) {
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    T g[3], vc = T(1);
+    plt_gradient<T>(P, i, j, kz, g, &vc);
+    out[4 * idx + 0] = g[0];
+    out[4 * idx + 1] = g[1];
+    out[4 * idx + 2] = g[2];
+    out[4 * idx + 3] = vc;
+  }
+}
+
 template <typename I>
 __global__ void k_ids(I* ids, int n, int overload, uint64_t offset) {
   const size_t n3 = (size_t)n * n * n;
@@ -150,6 +170,8 @@ struct mf_ic {
   void* phase = nullptr;  // exp(+2 pi i m / 2n), m in [0, 2n), grid precision
   double* qtab = nullptr; // lattice coordinates q[ishift][d][idx] * lunit
   void* plt = nullptr;    // PLT tables Dr, Dth, Dph, Dvf in the grid precision
+  void* pltg = nullptr;   // PLT gradient and vfac_corr per N-grid mode [idx][4]
+  double* stage = nullptr;  // n^3 doubles: host noise upload of an FP32 pipeline
   int plt_ng = 0;
   mf_conv* conv = nullptr;
   double* amp = nullptr;
@@ -611,6 +633,7 @@ int enqueue_impl(mf_ic* ic) {
           op.P.ng = ic->plt_ng;
           op.P.mapratio = T((double)ic->plt_ng / (double)n);
           op.P.inv_mr_L = T(1.0 / ((double)ic->plt_ng / (double)n) / L);
+          op.pg = (const T*)ic->pltg;
         }
         {
           LaunchScope ls(c, KK_FFT_COL);
@@ -728,7 +751,8 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   int64_t np; size_t pb, vb, ib;
   output_sizes(p, &np, &pb, &vb, &ib);
   const size_t nk2 = 3 * (size_t)(n / 2) * (n / 2) + 1;
-  *bytes = ngrids * grid + conv + pb + vb + ib + 2 * nk2 * sizeof(double);
+  const size_t pltg = p->plt ? 4 * (size_t)n * n * (n / 2 + 1) * ps : 0;
+  *bytes = ngrids * grid + conv + pb + vb + ib + 2 * nk2 * sizeof(double) + pltg;
   return MF_OK;
 }
 
@@ -745,6 +769,8 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->phase);
   cudaFree(ic->qtab);
   cudaFree(ic->plt);
+  cudaFree(ic->pltg);
+  cudaFree(ic->stage);
   if (ic->conv) mf_conv_destroy(ic->conv);
   if (ic->qx) mf_grid_destroy(ic->qx);
   cudaFree(ic->rf);
@@ -839,6 +865,25 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     cudaError_t e3 = cudaMalloc(&ic->plt, h.size());
     if (e3 == cudaSuccess) e3 = cudaMemcpy(ic->plt, h.data(), h.size(), cudaMemcpyHostToDevice);
     if (e3 != cudaSuccess) return fail(cuda_err(c, e3, "mf_ic_create: PLT tables"));
+    const size_t nmode = (size_t)n * n * (n / 2 + 1);
+    if ((e3 = cudaMalloc(&ic->pltg, 4 * nmode * es)) != cudaSuccess) return fail(cuda_err(c, e3, "mf_ic_create: PLT gradient"));
+    auto launch = [&](auto tag) {
+      using T = decltype(tag);
+      PLTDev<T> P;
+      const T* base = (const T*)ic->plt;
+      P.Dr = base;
+      P.Dth = base + nkt;
+      P.Dph = base + 2 * nkt;
+      P.Dvf = base + 3 * nkt;
+      P.ng = ic->plt_ng;
+      P.mapratio = T((double)ic->plt_ng / (double)n);
+      P.inv_mr_L = T(1.0 / ((double)ic->plt_ng / (double)n) / p->boxlen);
+      k_plt_grad_table<T><<<blocks_for(nmode), kThreads, 0, c->stream>>>((T*)ic->pltg, n, P);
+    };
+    if (es == sizeof(float)) launch(float{});
+    else launch(double{});
+    if ((e3 = cudaGetLastError()) == cudaSuccess) e3 = cudaStreamSynchronize(c->stream);
+    if (e3 != cudaSuccess) return fail(cuda_err(c, e3, "mf_ic_create: PLT gradient"));
   }
   if (uses_shared_sources(p)) {
     ic->shared = true;
@@ -894,14 +939,16 @@ extern "C" int mf_ic_set_noise(mf_ic* ic, const double* noise, int location) {
   const int n = ic->p.ngrid;
   const size_t n3 = (size_t)n * n * n;
   cudaError_t e = cudaSuccess;
-  if (location == MF_LOC_HOST) {
-    double* stage = nullptr;
-    e = cudaMallocAsync(&stage, n3 * sizeof(double), c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(stage, noise, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess)
-      e = (ic->p.precision == MF_PREC_F64) ? pw_fill_from_f64<double>((double*)ic->wn->d, stage, n, c->stream)
-                                           : pw_fill_from_f64<float>((float*)ic->wn->d, stage, n, c->stream);
-    if (stage) cudaFreeAsync(stage, c->stream);
+  if (location == MF_LOC_HOST && ic->p.precision == MF_PREC_F64) {
+    // rows of n doubles into the padded rows of n+2: one pitched copy
+    e = cudaMemcpy2DAsync(ic->wn->d, (size_t)(n + 2) * sizeof(double), noise, (size_t)n * sizeof(double),
+                          (size_t)n * sizeof(double), (size_t)n * n, cudaMemcpyHostToDevice, c->stream);
+  } else if (location == MF_LOC_HOST) {
+    // FP32 grid: through a staging buffer kept by the pipeline (allocated at the first host upload)
+    if (!ic->stage && (e = cudaMalloc((void**)&ic->stage, n3 * sizeof(double))) != cudaSuccess)
+      return cuda_err(c, e, "mf_ic_set_noise: staging buffer");
+    e = cudaMemcpyAsync(ic->stage, noise, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = pw_fill_from_f64<float>((float*)ic->wn->d, ic->stage, n, c->stream);
   } else {
     e = (ic->p.precision == MF_PREC_F64) ? pw_fill_from_f64<double>((double*)ic->wn->d, noise, n, c->stream)
                                          : pw_fill_from_f64<float>((float*)ic->wn->d, noise, n, c->stream);

@@ -308,6 +308,7 @@ struct AssembleXInvOp {
   int plt;          // PLT corrected gradient (lattice_gradient, particle_plt.hh:551-573)
   int vel;          // velocities: times the PLT growth-rate correction vfac_corr (:575-585)
   PLTDev<T> P;
+  const T* pg;  // tabulated PLT gradient and vfac_corr [idx][4] (nullptr: evaluate from P)
   static constexpr bool kPrefetch = false;
   static constexpr bool kPipe = false;
 
@@ -319,7 +320,15 @@ struct AssembleXInvOp {
     T gd, gp, gpp, vc = T(1);
     if (plt) {
       T g[3];
-      plt_gradient<T>(P, i, j, kz, g, vel ? &vc : nullptr);
+      if (pg) {
+        const T* q = pg + 4 * idx;
+        g[0] = q[0];
+        g[1] = q[1];
+        g[2] = q[2];
+        if (vel) vc = q[3];
+      } else {
+        plt_gradient<T>(P, i, j, kz, g, vel ? &vc : nullptr);
+      }
       gd = (d == 0) ? g[0] : ((d == 1) ? g[1] : g[2]);
       gp = (dp == 0) ? g[0] : ((dp == 1) ? g[1] : g[2]);
       gpp = (dpp == 0) ? g[0] : ((dpp == 1) ? g[1] : g[2]);
