@@ -328,11 +328,12 @@ int shared_sources(mf_ic* ic, bool timed) {
     return cudaSuccess;
   };
   struct Term { int a, b; double w; };
+  // products of at most this many distinct fields are formed inside the z pass
+  constexpr int kFusedProductFields = 0;
   const int pidx_field = (p.lpt_order > 2) ? 17 : 6;  // scratch field of the product sums
-  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2).
-  // With one or two distinct fields the product is formed inside the z pass;
-  // with more, a streaming pointwise kernel forms it first (every field read
-  // once at full bandwidth) and the z pass transforms the single sum.
+  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2):
+  // a streaming pointwise kernel forms the sum (every field read once at full
+  // bandwidth) and the TMA-pipelined z pass transforms it.
   auto prod = [&](std::initializer_list<Term> terms, cplx<T>* target, int op, int invlap) -> cudaError_t {
     ProdR2CZOp<T> po{};
     ProdSum<T> ps{};
@@ -356,7 +357,7 @@ int shared_sources(mf_ic* ic, bool timed) {
     po.dst = W[0];
     po.dst_stride = Kz;
     cudaError_t e2;
-    if (nd <= 2) {
+    if (nd <= kFusedProductFields) {
       LaunchScope ls(c, KK_CONV_Z);
       if ((e2 = Launch<T>::z_r2c_prod(H, po, M * M, Kz, twH, twM, s)) != cudaSuccess) return e2;
     } else {
@@ -364,10 +365,19 @@ int shared_sources(mf_ic* ic, bool timed) {
         LaunchScope ls(c, KK_POINTWISE);
         if ((e2 = pw_prodsum<T>((T*)R(pidx_field), 2 * rl, ps, s)) != cudaSuccess) return e2;
       }
+      ZConvArgs<T> za{};
+      za.in[0] = R(pidx_field);
+      za.out = W[0];
+      za.nop = 1;
+      za.kin = H;
+      za.kout = Kz;
+      za.in_stride = H;
+      za.out_stride = Kz;
+      za.nlines = M * M;
+      za.out_scale = T(1);
+      za.err = c->d_err;
       LaunchScope ls(c, KK_CONV_Z);
-      if ((e2 = Launch<T>::z_r2c_pad(H, PadR2CZOp<T>{R(pidx_field), H, W[0], Kz}, M * M, Kz, twH, twM, s)) !=
-          cudaSuccess)
-        return e2;
+      if ((e2 = Launch<T>::z_r2c_tma(H, za, twH, twM, s)) != cudaSuccess) return e2;
     }
     ConvYFwdOp<T> yf{W[0], W[0], g};
     {

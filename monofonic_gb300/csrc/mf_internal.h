@@ -79,6 +79,9 @@ struct Launch {
   // z_c2r_pad through the TMA-pipelined z pass (a.nop = 1, a.out = real field)
   static cudaError_t z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                                cudaStream_t s);
+  // z_r2c_pad through the TMA-pipelined z pass (a.nop = 1, a.in[0] = real field)
+  static cudaError_t z_r2c_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
+                               cudaStream_t s);
 };
 
 }  // namespace mf

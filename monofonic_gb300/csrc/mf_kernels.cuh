@@ -324,9 +324,12 @@ __device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin,
   return mkc<T>(Ev.x - Ov.y, Ev.y + Ov.x);
 }
 
-// C2R_ONLY: the inverse transform of one operand only, its real line
-// (M reals as H packed pairs) stored to out[line * out_stride + m]
-template <typename T, int H, int MAXR, int LPB, class SYNC, bool C2R_ONLY = false>
+// MODE 0: the fused convolution z pass above.
+// MODE 1: the inverse transform of one operand only, its real line (M reals
+//         as H packed pairs) stored to out[line * out_stride + m].
+// MODE 2: the forward transform of one real line (H packed pairs, kin = H),
+//         stored as kz < kout like MODE 0.
+template <typename T, int H, int MAXR, int LPB, class SYNC, int MODE = 0>
 __global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR, true>::TPL)
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
   using FI = LineFFT<T, H, true, MAXR, true>;
@@ -379,7 +382,12 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
       return;
     }
     C v[E], prod[E];
-    for (int op = 0; op < nop; ++op) {
+    if constexpr (MODE == 2) {
+      const C* src = stage + (st * nop) * per_op + ly * kin;
+#pragma unroll
+      for (int s = 0; s < E; ++s) v[s] = src[FF::in_index(t, s)];
+    }
+    for (int op = 0; op < nop && MODE != 2; ++op) {
       const C* src = stage + (st * nop + op) * per_op + ly * kin;
 #pragma unroll
       for (int s = 0; s < E; ++s) v[s] = c2r_pre_s<T, H>(src, FI::in_index(t, s), kin, twM);
@@ -392,17 +400,19 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
         for (int s = 0; s < E; ++s) { prod[s].x *= v[s].x; prod[s].y *= v[s].y; }
       }
     }
-    if constexpr (C2R_ONLY) {
+    if constexpr (MODE == 1) {
       C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
 #pragma unroll
       for (int s = 0; s < E; ++s) dst[FI::out_index(t, s)] = prod[s];
     } else {
-      sync();
+      if constexpr (MODE == 0) {
+        sync();
 #pragma unroll
-      for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
-      sync();
+        for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
+        sync();
 #pragma unroll
-      for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
+        for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
+      }
       FF::run(v, t, sm, 1, twH, sync);
       sync();
 #pragma unroll

@@ -145,12 +145,13 @@ constexpr int tma_lines_per_batch() {
 // lines is one 16-byte aligned contiguous block per operand, otherwise the
 // direct-load kernel.  Radix-4 plan (fewer registers per thread); warp
 // barriers when a line's threads fit in one warp.
-// C2R_ONLY: the shared-source inverse transform of one operand into a real
-// padded field (fallback: the direct-load plain c2r kernel)
-template <typename T, int H, bool C2R_ONLY = false>
+// MODE 1 / 2: the shared-source inverse transform of one operand into a real
+// padded field / forward transform of one real padded field (fallbacks: the
+// direct-load plain z kernels)
+template <typename T, int H, int MODE = 0>
 cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
   const PassSched sc = sched_get(KK_CONV_Z, 2 * H, (int)sizeof(T));
-  if (sc.variant == 0 || C2R_ONLY) {
+  if (sc.variant == 0 || MODE != 0) {
     // TMA path: radix-8-first plan with the padded (conflict-free) exchange layout
     constexpr int MAXR = MF_ZCONV_TMA_MAXR;
     constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
@@ -162,7 +163,7 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
                         (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
     if (tma_ok) {
-      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, C2R_ONLY>;
+      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE>;
       const size_t smem =
           128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * padded_len(H, true)) * sizeof(cplx<T>);
       cudaError_t e = set_smem(kern, smem);
@@ -181,8 +182,12 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
       return cudaGetLastError();
     }
   }
-  if constexpr (C2R_ONLY) {
+  if constexpr (MODE == 1) {
     return launch_zc2r<T, H>(PadC2RZOp<T>{a.in[0], a.in_stride, a.out, (int)a.out_stride}, a.nlines, a.kin, twH,
+                             twM, s);
+  }
+  if constexpr (MODE == 2) {
+    return launch_zr2c<T, H>(PadR2CZOp<T>{a.in[0], (int)a.in_stride, a.out, a.out_stride}, a.nlines, a.kout, twH,
                              twM, s);
   }
   // direct-load fallback: radix-4 plan, unpadded
@@ -305,10 +310,18 @@ cudaError_t Launch<T>::z_c2r_pad(int H, PadC2RZOp<T> op, int nlines, int kin, co
 template <typename T>
 cudaError_t Launch<T>::z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                                  cudaStream_t s) {
-#define CASE(HH) case HH: return launch_zconv<T, HH, true>(a, twH, twM, s);
+#define CASE(HH) case HH: return launch_zconv<T, HH, 1>(a, twH, twM, s);
   switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T>
+cudaError_t Launch<T>::z_r2c_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
+                                 cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zconv<T, HH, 2>(a, twH, twM, s);
+  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::z_r2c_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_c2r_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template <typename T>
 cudaError_t Launch<T>::z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
