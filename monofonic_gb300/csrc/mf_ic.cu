@@ -195,7 +195,7 @@ struct mf_ic {
   bool pos_copied = false;
   // shared-source convolutions: padded real fields and three work buffers
   bool shared = false;
-  void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last: product sums)
+  void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last 5 or 1: product sums)
   void* w3 = nullptr;   // three work buffers [M][M][N/2+1] complex
   mf_grid* qx = nullptr;  // fifth N-grid buffer of the phi(3) pair products
 };
@@ -327,55 +327,23 @@ int shared_sources(mf_ic* ic, bool timed) {
     }
     return cudaSuccess;
   };
-  struct Term { int a, b; double w; };
-  // products of at most this many distinct fields are formed inside the z pass
-  constexpr int kFusedProductFields = 0;
-  const int pidx_field = (p.lpt_order > 2) ? 17 : 6;  // scratch field of the product sums
-  // r2c of sum_t w_t R[a_t] R[b_t], unpadded into target with op:: (and -1/k^2):
-  // a streaming pointwise kernel forms the sum (every field read once at full
-  // bandwidth) and the TMA-pipelined z pass transforms it.
-  auto prod = [&](std::initializer_list<Term> terms, cplx<T>* target, int op, int invlap) -> cudaError_t {
-    ProdR2CZOp<T> po{};
-    ProdSum<T> ps{};
-    int t = 0, distinct[2 * kMaxProdTerms], nd = 0;
-    for (const Term& tm : terms) {
-      po.fa[t] = R(tm.a);
-      po.fb[t] = R(tm.b);
-      po.w[t] = T(tm.w);
-      ps.fa[t] = (const T*)R(tm.a);
-      ps.fb[t] = (const T*)R(tm.b);
-      ps.w[t] = T(tm.w);
-      for (int f : {tm.a, tm.b}) {
-        bool seen = false;
-        for (int q = 0; q < nd; ++q) seen |= distinct[q] == f;
-        if (!seen) distinct[nd++] = f;
-      }
-      ++t;
-    }
-    po.nterm = ps.nterm = t;
-    po.H = H;
-    po.dst = W[0];
-    po.dst_stride = Kz;
+  // product-sum scratch fields (after the 17 operand fields)
+  const int P0 = (p.lpt_order > 2) ? 17 : 6;
+  // TMA r2c of real field `src`, unpadded into target with op:: (and -1/k^2)
+  auto r2c_unpad = [&](int src, cplx<T>* target, int op, int invlap) -> cudaError_t {
+    ZConvArgs<T> za{};
+    za.in[0] = R(src);
+    za.out = W[0];
+    za.nop = 1;
+    za.kin = H;
+    za.kout = Kz;
+    za.in_stride = H;
+    za.out_stride = Kz;
+    za.nlines = M * M;
+    za.out_scale = T(1);
+    za.err = c->d_err;
     cudaError_t e2;
-    if (nd <= kFusedProductFields) {
-      LaunchScope ls(c, KK_CONV_Z);
-      if ((e2 = Launch<T>::z_r2c_prod(H, po, M * M, Kz, twH, twM, s)) != cudaSuccess) return e2;
-    } else {
-      {
-        LaunchScope ls(c, KK_POINTWISE);
-        if ((e2 = pw_prodsum<T>((T*)R(pidx_field), 2 * rl, ps, s)) != cudaSuccess) return e2;
-      }
-      ZConvArgs<T> za{};
-      za.in[0] = R(pidx_field);
-      za.out = W[0];
-      za.nop = 1;
-      za.kin = H;
-      za.kout = Kz;
-      za.in_stride = H;
-      za.out_stride = Kz;
-      za.nlines = M * M;
-      za.out_scale = T(1);
-      za.err = c->d_err;
+    {
       LaunchScope ls(c, KK_CONV_Z);
       if ((e2 = Launch<T>::z_r2c_tma(H, za, twH, twM, s)) != cudaSuccess) return e2;
     }
@@ -396,11 +364,18 @@ int shared_sources(mf_ic* ic, bool timed) {
     LaunchScope ls(c, KK_CONV_XFWD);
     return Launch<T>::conv_xfwd(M, xf, N, Kz, twM, s);
   };
-  // Hessian field index: (0,0) (1,1) (2,2) (0,1) (0,2) (1,2)
-  auto hx = [](int a, int b) {
-    if (a > b) { const int t = a; a = b; b = t; }
-    return (a == b) ? a : (a == 0 ? (b == 1 ? 3 : 4) : 5);
+  // the streaming product kernel of one source set (mf_sources.cu) into P0, P0+1, ...
+  auto sources = [&](int set) -> cudaError_t {
+    const T* fields[kSrcFields] = {};
+    for (int f = 0; f < kSrcFields; ++f)
+      if (f < P0) fields[f] = (const T*)R(f);
+    T* outs[kSrcOutputs] = {};
+    for (int o = 0; o < kSrcOutputs; ++o)
+      if (P0 + o < ((p.lpt_order > 2) ? 22 : 7)) outs[o] = (T*)R(P0 + o);
+    LaunchScope ls(c, KK_POINTWISE);
+    return pw_sources<T>(set, fields, outs, 2 * rl, s);
   };
+  // Hessian fields in the order (0,0) (1,1) (2,2) (0,1) (0,2) (1,2)
   const int HD[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   auto hessians = [&](int fi, int base) -> cudaError_t {
     for (int half = 0; half < 2; ++half) {
@@ -422,8 +397,8 @@ int shared_sources(mf_ic* ic, bool timed) {
 
   // ---- phi(2) (ic_generator.cc:471-488) ----------------------------------
   CK(hessians(0, 0));
-  CK(prod({{0, 1, 1.0}, {0, 2, 1.0}, {1, 2, 1.0}, {3, 3, -1.0}, {4, 4, -1.0}, {5, 5, -1.0}},
-          (cplx<T>*)ic->f[1]->d, OUT_ASSIGN, 1));
+  CK(sources(SRC_PHI2));
+  CK(r2c_unpad(P0, (cplx<T>*)ic->f[1]->d, OUT_ASSIGN, 1));
   ic->f[1]->space = MF_SPACE_K;
   if (timed) CK(cudaEventRecord(ic->ev[2], s));
   if (p.lpt_order > 2) {
@@ -432,8 +407,8 @@ int shared_sources(mf_ic* ic, bool timed) {
     // convolve3 first stages: truncated pair products phi,00 phi,11 / phi,01 phi,02 /
     // phi,12^2 / phi,02^2 / phi,01^2, then their padded c2r
     mf_grid* qg[5] = {ic->tmp[0], ic->tmp[1], ic->tmp[2], ic->wn, ic->qx};
-    const int pa[5][2] = {{0, 1}, {3, 4}, {5, 5}, {4, 4}, {3, 3}};
-    for (int k = 0; k < 5; ++k) CK(prod({{pa[k][0], pa[k][1], 1.0}}, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
+    CK(sources(SRC_PAIRS));
+    for (int k = 0; k < 5; ++k) CK(r2c_unpad(P0 + k, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
     {
       Operand<T> ops[3];
       int dst[3];
@@ -448,20 +423,13 @@ int shared_sources(mf_ic* ic, bool timed) {
         CK(c2r(nb, ops, dst));
       }
     }
-    const double a5 = -5.0 / 7.0, a10 = 10.0 / 7.0;
-    CK(prod({{12, 2, 1.0}, {13, 5, 2.0}, {14, 0, -1.0}, {15, 1, -1.0}, {16, 2, -1.0},
-             {0, 7, a5}, {0, 8, a5}, {1, 8, a5}, {1, 6, a5}, {2, 6, a5}, {2, 7, a5},
-             {3, 9, a10}, {4, 10, a10}, {5, 11, a10}},
-            (cplx<T>*)ic->f[2]->d, OUT_ASSIGN, 1));
+    CK(sources(SRC_PHI3_A3));
+    CK(r2c_unpad(P0, (cplx<T>*)ic->f[2]->d, OUT_ASSIGN, 1));
     ic->f[2]->space = MF_SPACE_K;
     if (timed) CK(cudaEventRecord(ic->ev[3], s));
     // ---- A(3) (ic_generator.cc:534-545) ---------------------------------
     for (int d = 0; d < 3; ++d) {
-      const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
-      CK(prod({{6 + hx(d, dp), hx(d, dpp), 1.0}, {6 + hx(d, dpp), hx(d, dp), -1.0},
-               {hx(dp, dpp), 6 + hx(dp, dp), 1.0}, {hx(dp, dpp), 6 + hx(dpp, dpp), -1.0},
-               {6 + hx(dp, dpp), hx(dp, dp), -1.0}, {6 + hx(dp, dpp), hx(dpp, dpp), 1.0}},
-              (cplx<T>*)ic->f[3 + d]->d, OUT_ASSIGN, 1));
+      CK(r2c_unpad(P0 + 1 + d, (cplx<T>*)ic->f[3 + d]->d, OUT_ASSIGN, 1));
       ic->f[3 + d]->space = MF_SPACE_K;
     }
   } else if (timed) {
@@ -751,7 +719,7 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   if (p->lpt_order > 1) {
     const size_t M = (p->convolver == MF_CONV_ORSZAG) ? 3 * n / 2 : n;
     if (uses_shared_sources(p)) {
-      const size_t nreal = (p->lpt_order > 2) ? 18 : 7;
+      const size_t nreal = (p->lpt_order > 2) ? 22 : 7;
       conv = 3 * M * M * (n / 2 + 1) * 2 * ps + nreal * M * M * M * ps + (p->lpt_order > 2 ? grid : 0);
     } else {
       const int nbuf = (p->convolver == MF_CONV_ORSZAG) ? 2 : 3;
@@ -898,7 +866,7 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   if (uses_shared_sources(p)) {
     ic->shared = true;
     const size_t M = 3 * (size_t)n / 2, cs = (p->precision == MF_PREC_F32) ? sizeof(float2) : sizeof(double2);
-    const size_t nreal = (p->lpt_order > 2) ? 18 : 7;  // operands + the product-sum scratch field
+    const size_t nreal = (p->lpt_order > 2) ? 22 : 7;  // operands + the product-sum scratch fields
     cudaError_t e4 = cudaMalloc(&ic->rf, nreal * M * M * (M / 2) * cs);
     if (e4 == cudaSuccess) e4 = cudaMalloc(&ic->w3, 3 * M * M * (n / 2 + 1) * cs);
     if (e4 != cudaSuccess) return fail(cuda_err(c, e4, "mf_ic_create: shared-source buffers"));

@@ -69,17 +69,11 @@ struct Launch {
                                  const cplx<T>* twM, cudaStream_t s);
   static cudaError_t z_conv(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                             cudaStream_t s);
-  // z passes of the shared-source convolutions (padded lengths)
-  static cudaError_t z_c2r_pad(int H, PadC2RZOp<T> op, int nlines, int kin, const cplx<T>* twH,
-                               const cplx<T>* twM, cudaStream_t s);
-  static cudaError_t z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
-                                const cplx<T>* twM, cudaStream_t s);
-  static cudaError_t z_r2c_pad(int H, PadR2CZOp<T> op, int nlines, int kout, const cplx<T>* twH,
-                               const cplx<T>* twM, cudaStream_t s);
-  // z_c2r_pad through the TMA-pipelined z pass (a.nop = 1, a.out = real field)
+  // z passes of the shared-source convolutions (padded lengths):
+  // c2r of one operand line set into a real padded field (a.nop = 1, a.out = real field)
   static cudaError_t z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                                cudaStream_t s);
-  // z_r2c_pad through the TMA-pipelined z pass (a.nop = 1, a.in[0] = real field)
+  // r2c of one real padded field, kz < a.kout kept (a.nop = 1, a.in[0] = real field)
   static cudaError_t z_r2c_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                                cudaStream_t s);
 };

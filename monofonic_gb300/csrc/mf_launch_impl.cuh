@@ -301,13 +301,6 @@ cudaError_t Launch<T>::z_conv(int H, const ZConvArgs<T>& a, const cplx<T>* twH, 
 }
 template cudaError_t Launch<MF_T>::z_conv(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template <typename T>
-cudaError_t Launch<T>::z_c2r_pad(int H, PadC2RZOp<T> op, int nlines, int kin, const cplx<T>* twH,
-                                 const cplx<T>* twM, cudaStream_t s) {
-#define CASE(HH) case HH: return launch_zc2r<T, HH>(op, nlines, kin, twH, twM, s);
-  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
-#undef CASE
-}
-template <typename T>
 cudaError_t Launch<T>::z_c2r_tma(int H, const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T>* twM,
                                  cudaStream_t s) {
 #define CASE(HH) case HH: return launch_zconv<T, HH, 1>(a, twH, twM, s);
@@ -321,25 +314,8 @@ cudaError_t Launch<T>::z_r2c_tma(int H, const ZConvArgs<T>& a, const cplx<T>* tw
   switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
-template cudaError_t Launch<MF_T>::z_r2c_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_c2r_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
-template <typename T>
-cudaError_t Launch<T>::z_r2c_prod(int H, const ProdR2CZOp<T>& op, int nlines, int kout, const cplx<T>* twH,
-                                  const cplx<T>* twM, cudaStream_t s) {
-#define CASE(HH) case HH: return launch_zr2c<T, HH>(op, nlines, kout, twH, twM, s);
-  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
-#undef CASE
-}
-template <typename T>
-cudaError_t Launch<T>::z_r2c_pad(int H, PadR2CZOp<T> op, int nlines, int kout, const cplx<T>* twH,
-                                 const cplx<T>* twM, cudaStream_t s) {
-#define CASE(HH) case HH: return launch_zr2c<T, HH>(op, nlines, kout, twH, twM, s);
-  switch (H) { MF_LEN_CONVH(CASE) default: return cudaErrorInvalidValue; }
-#undef CASE
-}
-template cudaError_t Launch<MF_T>::z_r2c_pad(int, PadR2CZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
-template cudaError_t Launch<MF_T>::z_c2r_pad(int, PadC2RZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
-template cudaError_t Launch<MF_T>::z_r2c_prod(int, const ProdR2CZOp<MF_T>&, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::z_r2c_tma(int, const ZConvArgs<MF_T>&, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 #endif
 
 }  // namespace mf

@@ -442,37 +442,6 @@ struct PadC2RZOp {
   __device__ __forceinline__ void store_pair(int line, int m, C v) const { dst[(long long)line * H + m] = v; }
 };
 
-// z pass r2c of a sum of products of real fields,
-// p(x) = sum_t w_t F_{a_t}(x) F_{b_t}(x), keeping kz < kout.  Per-term field
-// pointers (rather than indices into a field table) keep every parameter
-// access static once the term loop is unrolled.
-constexpr int kMaxProdTerms = 16;
-template <typename T>
-struct ProdR2CZOp {
-  using C = cplx<T>;
-  const C* fa[kMaxProdTerms];
-  const C* fb[kMaxProdTerms];
-  T w[kMaxProdTerms];
-  int nterm;
-  int H;
-  C* dst;
-  long long dst_stride;  // Kz
-  __device__ __forceinline__ C load_pair(int line, int m) const {
-    const long long o = (long long)line * H + m;
-    T px = T(0), py = T(0);
-#pragma unroll
-    for (int t = 0; t < kMaxProdTerms; ++t) {
-      if (t < nterm) {
-        const C x = fa[t][o], y = fb[t][o];
-        px += w[t] * (x.x * y.x);
-        py += w[t] * (x.y * y.y);
-      }
-    }
-    return mkc<T>(px, py);
-  }
-  __device__ __forceinline__ void store(int line, int k, C v) const { dst[line * dst_stride + k] = v; }
-};
-
 // z pass r2c of one real padded field, keeping kz < kout
 template <typename T>
 struct PadR2CZOp {
@@ -483,15 +452,6 @@ struct PadR2CZOp {
   long long dst_stride;  // Kz
   __device__ __forceinline__ C load_pair(int line, int m) const { return src[(long long)line * H + m]; }
   __device__ __forceinline__ void store(int line, int k, C v) const { dst[line * dst_stride + k] = v; }
-};
-
-// pointwise sum of products of real fields, out = sum_t w_t a_t b_t
-template <typename T>
-struct ProdSum {
-  const T* fa[kMaxProdTerms];
-  const T* fb[kMaxProdTerms];
-  T w[kMaxProdTerms];
-  int nterm;
 };
 
 // arguments of the fused Orszag z pass (mf_kernels.cuh, k_zconv)

@@ -67,31 +67,6 @@ __global__ void k_white_noise(T* d, int n, unsigned long long seed, const unsign
   }
 }
 
-// sum of products of real fields, 16-byte vectors, memory-bound streaming
-template <typename T>
-__global__ void __launch_bounds__(256) k_prodsum(T* __restrict__ out, size_t nvec, ProdSum<T> ps) {
-  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-  constexpr int W = 16 / sizeof(T);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nvec; i += (size_t)gridDim.x * blockDim.x) {
-    T acc[W] = {};
-#pragma unroll
-    for (int t = 0; t < kMaxProdTerms; ++t) {
-      if (t < ps.nterm) {
-        const V a = reinterpret_cast<const V*>(ps.fa[t])[i], b = reinterpret_cast<const V*>(ps.fb[t])[i];
-        const T* ae = reinterpret_cast<const T*>(&a);
-        const T* be = reinterpret_cast<const T*>(&b);
-#pragma unroll
-        for (int j = 0; j < W; ++j) acc[j] += ps.w[t] * (ae[j] * be[j]);
-      }
-    }
-    V r;
-    T* re = reinterpret_cast<T*>(&r);
-#pragma unroll
-    for (int j = 0; j < W; ++j) re[j] = acc[j];
-    reinterpret_cast<V*>(out)[i] = r;
-  }
-}
-
 // shift_field's phase (grid_fft.hh:835-838): x * exp(i (s.k) dx)
 template <typename T>
 __global__ void k_shift(cplx<T>* d, int n, T kfac, T dx, T s0, T s1, T s2) {
@@ -178,20 +153,6 @@ cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s) {
   return cudaGetLastError();
 }
 template <typename T>
-cudaError_t pw_prodsum(T* out, size_t n, const ProdSum<T>& ps, cudaStream_t s) {
-  constexpr size_t W = 16 / sizeof(T);
-  if (n % W) return cudaErrorInvalidValue;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const size_t nvec = n / W;
-  size_t grid = (nvec + 255) / 256;
-  const size_t cap = (size_t)nsm * 8;  // 8 resident CTAs of 256 threads per SM
-  if (grid > cap) grid = cap;
-  k_prodsum<T><<<(unsigned)(grid ? grid : 1), 256, 0, s>>>(out, nvec, ps);
-  return cudaGetLastError();
-}
-template <typename T>
 cudaError_t pw_white_noise(T* d, int n, unsigned long long seed, const unsigned long long* seed_dev, cudaStream_t s) {
   if (n <= 0 || (n & 1)) return cudaErrorInvalidValue;
   k_white_noise<T><<<grid_for((size_t)n * n * (n / 2), 2), kThreads, 0, s>>>(d, n, seed, seed_dev);
@@ -215,7 +176,6 @@ cudaError_t pw_power_spectrum(const cplx<T>* d, int n, double kfac, int nbins, d
   template cudaError_t pw_shift<T>(cplx<T>*, int, double, double, const double*, cudaStream_t);      \
   template cudaError_t pw_fill_from_f64<T>(T*, const double*, int, cudaStream_t);                    \
   template cudaError_t pw_white_noise<T>(T*, int, unsigned long long, const unsigned long long*, cudaStream_t); \
-  template cudaError_t pw_prodsum<T>(T*, size_t, const ProdSum<T>&, cudaStream_t);                       \
   template cudaError_t pw_power_spectrum<T>(const cplx<T>*, int, double, int, double*, cudaStream_t);
 INST(float)
 INST(double)

@@ -102,8 +102,14 @@ template <typename T> cudaError_t pw_zero_dc(T* d, cudaStream_t s);
 template <typename T> cudaError_t pw_invlap(cplx<T>* d, int n, double kfac, cudaStream_t s);
 template <typename T> cudaError_t pw_shift(cplx<T>* d, int n, double kfac, double dx, const double sh[3], cudaStream_t s);
 template <typename T> cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s);
-// out[i] = sum_t w_t fa_t[i] fb_t[i] over n reals (n a multiple of 4)
-template <typename T> cudaError_t pw_prodsum(T* out, size_t n, const ProdSum<T>& ps, cudaStream_t s);
+// LPT source products over the shared padded real fields (mf_sources.cu):
+// fields[0..16] (Hessians of phi, of phi(2), convolve3 pair products), outs
+// the product sums of the set: SRC_PHI2 1, SRC_PAIRS 5, SRC_PHI3_A3 4
+enum { SRC_PHI2 = 0, SRC_PAIRS = 1, SRC_PHI3_A3 = 2 };
+constexpr int kSrcFields = 17, kSrcOutputs = 5;
+template <typename T>
+cudaError_t pw_sources(int set, const T* const* fields, T* const* outs, size_t n, cudaStream_t s);
+
 // project RNG plugin on the device (bit-identical to mf_white_noise_host);
 // seed from *seed_dev when it is not null
 template <typename T>
