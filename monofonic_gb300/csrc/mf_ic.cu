@@ -578,7 +578,31 @@ int enqueue_impl(mf_ic* ic) {
     }
     CK(cudaGetLastError());
     void* dst = vel ? ic->dvel : ic->dpos;
+    const bool three = Launch<T>::assemble3_supported(n);
     for (int ish = 0; ish < overload; ++ish) {
+      if (three) {  // x pass of the three components in one launch
+        Assemble3XInvOp<T> op{};
+        op.phitot = (const cplx<T>*)wsum;
+        for (int d = 0; d < 3; ++d) {
+          op.A3[d] = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + d]->d : nullptr;
+          op.dst[d] = (cplx<T>*)ic->tmp[d]->d;
+        }
+        op.phase = (const cplx<T>*)ic->phase;
+        op.n = n;
+        op.Kz = Kz;
+        op.nstep = ish;
+        for (int st = 1; st <= ish; ++st)
+          for (int q = 0; q < 3; ++q)
+            op.s2[st - 1][q] = (int)lround(2 * (kShifts[p.lattice][st][q] - kShifts[p.lattice][st - 1][q]));
+        op.kfac = T(kfac);
+        op.wA = &ic->dyn_d->w[pass][3];
+        op.unit = T((vel ? p.vunit : p.lunit) / L);
+        op.plt = p.plt;
+        op.vel = vel ? 1 : 0;
+        op.pg = (const T*)ic->pltg;
+        LaunchScope ls(c, KK_FFT_COL);
+        CK(Launch<T>::assemble3_xinv(n, op, n, Kz, twN, s));
+      }
       for (int d = 0; d < 3; ++d) {
         T* tmpr = (T*)ic->tmp[d]->d;
         cplx<T>* tk = (cplx<T>*)tmpr;
@@ -613,7 +637,7 @@ int enqueue_impl(mf_ic* ic) {
           op.P.inv_mr_L = T(1.0 / ((double)ic->plt_ng / (double)n) / L);
           op.pg = (const T*)ic->pltg;
         }
-        {
+        if (!three) {
           LaunchScope ls(c, KK_FFT_COL);
           CK(Launch<T>::assemble_xinv(n, op, n, Kz, twN, s));
         }

@@ -54,6 +54,10 @@ struct Launch {
                                   const cplx<T>* tw, cudaStream_t s);
   static cudaError_t assemble_xinv(int L, AssembleXInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                    cudaStream_t s);
+  // all three components in one launch (lengths whose plan keeps E <= 8)
+  static bool assemble3_supported(int L);
+  static cudaError_t assemble3_xinv(int L, Assemble3XInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                    cudaStream_t s);
   static cudaError_t conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
                                const cplx<T>* tw, cudaStream_t s);
   static cudaError_t conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,

@@ -66,6 +66,39 @@ k_colfft(OP op, const cplx<T>* __restrict__ tw, int ncols) {
   }
 }
 
+// strided pass producing three transforms per column (three-component
+// assembly): the loader yields the three inputs of each element at once, the
+// three line FFTs run one after the other through the same shared tile
+template <typename T, int L, bool INV, int NCOL, class OP>
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV>::TPL)
+k_colfft3(OP op, const cplx<T>* __restrict__ tw, int ncols) {
+  using F = LineFFT<T, L, INV>;
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* sm = reinterpret_cast<C*>(smem_raw);
+  const int c = threadIdx.x, t = threadIdx.y;
+  const int col = blockIdx.x * NCOL + c;
+  const int slab = blockIdx.y;
+  const bool valid = col < ncols;
+  C v[3][F::E];
+#pragma unroll
+  for (int s = 0; s < F::E; ++s) {
+    C w[3] = {mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0))};
+    if (valid) op.load3(slab, F::in_index(t, s), col, w);
+    v[0][s] = w[0];
+    v[1][s] = w[1];
+    v[2][s] = w[2];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    F::run(v[d], t, sm + c, NCOL, tw, SyncBlock{});
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) op.store(d, slab, F::out_index(t, s), col, v[d][s]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // persistent, double-buffered strided pass.  Each CTA walks tiles
 // (column tile, slab, operand) with stride gridDim.x; while a tile is being

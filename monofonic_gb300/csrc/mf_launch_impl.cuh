@@ -247,6 +247,39 @@ cudaError_t Launch<T>::assemble_xinv(int L, AssembleXInvOp<T> op, int nslab, int
   switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T, int L>
+cudaError_t launch_col3(Assemble3XInvOp<T> op, int nslab, int ncols, const cplx<T>* tw, cudaStream_t s) {
+  if constexpr (LineFFT<T, L, true>::E > 8) {
+    return cudaErrorInvalidValue;  // three register sets of E > 8 elements: per-component passes instead
+  } else {
+    // at most 512 threads, so that the three register sets fit without spilling
+    constexpr int TPL = LineFFT<T, L, true>::TPL;
+    constexpr int NC0 = col_ncol<T, L>();
+    constexpr int NC = (NC0 * TPL > 512) ? ((512 / TPL) > 0 ? 512 / TPL : 1) : NC0;
+    const size_t smem = (size_t)L * NC * sizeof(cplx<T>);
+    auto kern = k_colfft3<T, L, true, NC, Assemble3XInvOp<T>>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, 1);
+    kern<<<grid, block, smem, s>>>(op, tw, ncols);
+    return cudaGetLastError();
+  }
+}
+template <typename T>
+bool Launch<T>::assemble3_supported(int L) {
+#define CASE(LL) case LL: return LineFFT<T, LL, true>::E <= 8;
+  switch (L) { MF_LEN_N(CASE) default: return false; }
+#undef CASE
+}
+template <typename T>
+cudaError_t Launch<T>::assemble3_xinv(int L, Assemble3XInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                      cudaStream_t s) {
+#define CASE(LL) case LL: return launch_col3<T, LL>(op, nslab, ncols, tw, s);
+  switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template bool Launch<MF_T>::assemble3_supported(int);
+template cudaError_t Launch<MF_T>::assemble3_xinv(int, Assemble3XInvOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::colfft_plain(int, bool, PlainStridedOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::assemble_xinv(int, AssembleXInvOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::z_r2c_plain(int, PlainZOp<MF_T>, int, int, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);

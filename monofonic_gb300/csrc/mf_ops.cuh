@@ -430,6 +430,103 @@ struct PlainZOp {
 // is transformed to real space once and kept in HBM as lines of M reals,
 // stored as H = M/2 packed pairs [line][H], line = x*M + y.
 
+// the x pass of all three displacement / velocity components of one
+// sub-lattice in one launch: the same k-space combination and sub-lattice
+// phase chain as AssembleXInvOp, with the order sum, the three A3 fields and
+// the gradient read once per mode for the three components
+template <typename T>
+struct Assemble3XInvOp {
+  using C = cplx<T>;
+  const C* phitot;
+  const C* A3[3];  // nullptr below 3LPT
+  C* dst[3];
+  const C* phase;
+  int n, Kz;
+  int nstep;
+  int s2[7][3];
+  T kfac, unit;
+  const double* wA;
+  int plt, vel;
+  const T* pg;  // tabulated PLT gradient and vfac_corr [idx][4]
+  __device__ __forceinline__ void assemble(int i, int j, int kz, C (&o)[3]) const {
+    const long long idx = ((long long)i * n + j) * Kz + kz;
+    if (idx == 0) {
+      o[0] = o[1] = o[2] = mkc<T>(T(0), T(0));
+      return;
+    }
+    T g[3], vc = T(1);
+    if (plt) {
+      const T* q = pg + 4 * idx;
+      g[0] = q[0];
+      g[1] = q[1];
+      g[2] = q[2];
+      if (vel) vc = q[3];
+    } else {
+      g[0] = gradk<T>(i, n, kfac);
+      g[1] = gradk<T>(j, n, kfac);
+      g[2] = gradk<T>(kz, n, kfac);
+    }
+    const C P1 = phitot[idx];
+    C X[3] = {mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0))};
+    T w = T(0);
+    if (A3[0]) {
+      X[0] = A3[0][idx];
+      X[1] = A3[1][idx];
+      X[2] = A3[2][idx];
+      w = T(__ldg(wA));
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int dp = (d + 1) % 3, dpp = (d + 2) % 3;
+      T rr = -g[d] * P1.y, ri = g[d] * P1.x;
+      if (A3[0]) {
+        rr += w * (-(g[dp] * X[dpp].y) + g[dpp] * X[dp].y);
+        ri += w * (g[dp] * X[dpp].x - g[dpp] * X[dp].x);
+      }
+      if (plt && vel) {
+        rr *= vc;
+        ri *= vc;
+      }
+      o[d] = mkc<T>(rr * unit, ri * unit);
+    }
+  }
+  __device__ __forceinline__ C step_phase(int s, int i, int j, int kz) const {
+    const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
+    int m = (s2[s][0] * ii + s2[s][1] * jj + s2[s][2] * kz) % (2 * n);
+    if (m < 0) m += 2 * n;
+    return phase[m];
+  }
+  // slab = j, e = i, col = kz
+  __device__ __forceinline__ void load3(int j, int i, int kz, C (&v)[3]) const {
+    assemble(i, j, kz, v);
+    if (nstep == 0) return;
+    if (kz == 0 || kz == (n >> 1)) {
+      const int im = (n - i) % n, jm = (n - j) % n;
+      C vm[3];
+      assemble(im, jm, kz, vm);
+      for (int s = 0; s < nstep; ++s) {
+        const C pk = step_phase(s, i, j, kz), pm = step_phase(s, im, jm, kz);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const C hk = mkc<T>(T(0.5) * (v[d].x + vm[d].x), T(0.5) * (v[d].y - vm[d].y));
+          const C hm = mkc<T>(T(0.5) * (vm[d].x + v[d].x), T(0.5) * (vm[d].y - v[d].y));
+          v[d] = cmul(hk, pk);
+          vm[d] = cmul(hm, pm);
+        }
+      }
+      return;
+    }
+    for (int s = 0; s < nstep; ++s) {
+      const C ph = step_phase(s, i, j, kz);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = cmul(v[d], ph);
+    }
+  }
+  __device__ __forceinline__ void store(int d, int j, int i, int kz, C v) const {
+    dst[d][((long long)i * n + j) * Kz + kz] = v;
+  }
+};
+
 // z pass c2r of a work-buffer line [line][Kz] (kz > N/2 zero) into a real line
 template <typename T>
 struct PadC2RZOp {
