@@ -123,33 +123,44 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # algorithmic bytes per launch of each kernel kind for one 3LPT IC
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(kind: str, n: int, prec_bytes: int) -> float:
+def algorithmic_bytes_ic(n: int, prec_bytes: int, overload: int = 2, plt: bool = True) -> dict:
+    """Unique bytes each kernel kind must read and write for one 3LPT IC of the
+    shared-source pipeline (each element once; re-reads not counted):
+    17 operands through the padded c2r (x, y, z passes), 10 product sums
+    through the padded r2c (z, y, x passes), the streaming source products,
+    and the assembly of `overload` sub-lattices for positions and velocities."""
     cs = 2 * prec_bytes
     M, Kz = 3 * n // 2, n // 2 + 1
     S_NK, S_MNK, S_MMK = n * n * Kz * cs, M * n * Kz * cs, M * M * Kz * cs
-    if kind == "conv_xinv":
-        return 2 * (S_NK + S_MNK)
-    if kind == "conv_yinv":
-        return 2 * (S_MNK + S_MMK)
-    if kind == "conv_z":
-        return 2 * S_MMK + S_MMK
-    if kind == "conv_yfwd":
-        return S_MMK + S_MNK
-    if kind == "conv_xfwd":
-        # 33 per 3LPT IC: 10 assign (write only), 23 read-modify-write
-        return S_MNK + (10 * S_NK + 23 * 2 * S_NK) / 33.0
-    if kind == "fft_z":
-        return 2 * n * n * (n + 2) * prec_bytes
-    if kind == "fft_col":
-        return 2 * S_NK
-    return float("nan")
+    S_R = M * M * M * prec_bytes  # padded real field
+    S_N = n * n * (n + 2) * prec_bytes  # N-grid
+    npart = overload * n ** 3
+    out = {
+        "conv_xinv": 17 * (S_NK + S_MNK),
+        "conv_yinv": 17 * (S_MNK + S_MMK),
+        "conv_z": 27 * (S_MMK + S_R),
+        "conv_yfwd": 10 * (S_MMK + S_MNK),
+        "conv_xfwd": 10 * (S_MNK + S_NK),
+        # noise r2c z pass + per sub-lattice and pass three component c2r z passes
+        "fft_z": (1 + 2 * overload * 3) * 2 * S_N,
+        # noise r2c y/x passes, three-component assembly x passes (order sum, A3 x3,
+        # PLT table of 4 reals per mode, three outputs), component y passes
+        "fft_col": 2 * 2 * S_NK + 2 * overload * ((1 + 3 + 3) * S_NK + (2 * S_NK if plt else 0))
+                   + 2 * overload * 3 * 2 * S_NK,
+        # source products (7 + 10 + 21 real fields), two FP64 order sums (3 in, 1 out),
+        # lattice readout (3 component grids in, AoS positions/velocities out), ids
+        "pointwise": (7 + 10 + 21) * S_R + 2 * 4 * S_NK
+                     + 2 * overload * 3 * S_N + 2 * npart * 3 * prec_bytes + npart * 8,
+    }
+    return out
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch from
 # ncu captures of smaller cases, per unit of work (M^2 (N/2+1) line-modes of
 # the padded work buffer), so that it scales to the bench's grid size
 TRAFFIC_PER_UNIT = {
-    ("conv_z", 4): (408.3e6 / (384 * 384 * 129), "ncu --set full, k_zconv_tma N=256 (M=384) FP32, one launch"),
+    ("conv_z", 4): (325.9e6 / (384 * 384 * 384), "ncu --set full, k_zconv_tma (c2r of one operand into a real "
+                                                 "padded field) N=256 (M=384) FP32, one launch"),
 }
 
 
@@ -157,8 +168,8 @@ def traffic_per_launch(kind: str, n: int, prec_bytes: int):
     t = TRAFFIC_PER_UNIT.get((kind, prec_bytes))
     if t is None:
         return None, None
-    M, Kz = 3 * n // 2, n // 2 + 1
-    return t[0] * M * M * Kz, t[1] + f", scaled to N={n} by M^2 (N/2+1)"
+    M = 3 * n // 2
+    return t[0] * M * M * M, t[1] + f", scaled to N={n} by M^3"
 
 
 def measured_peaks():
@@ -458,14 +469,15 @@ def run_mf(args):
     dom = max((k for k in prof if k != "pointwise"), key=lambda k: prof[k][0])
     dom_ms, dom_cnt = prof[dom]
     avg_ms = dom_ms / max(dom_cnt, 1)
-    bpl = algorithmic_bytes(dom, n, 4)
+    alg = algorithmic_bytes_ic(n, 4, overload=2, plt=True)
+    steps_prof = args.steps  # the profiled region covers every timed step
+    bpl = alg[dom] * steps_prof / max(dom_cnt, 1)  # algorithmic bytes per launch of the dominant kind
     achieved = bpl / (avg_ms / 1e3) / 1e9
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     kinds = {k: {"ms_total": round(v[0], 3), "launches": v[1],
                  "share": round(v[0] / max(sum(x[0] for x in prof.values()), 1e-9), 4),
-                 "GB_s": (round(algorithmic_bytes(k, n, 4) / (v[0] / max(v[1], 1) / 1e3) / 1e9, 1)
-                          if v[1] and k != "pointwise" else None)}
+                 "GB_s": (round(alg[k] * steps_prof / (v[0] / 1e3) / 1e9, 1) if v[0] > 0 and k in alg else None)}
              for k, v in prof.items()}
 
     # ---- e2e through the C ABI with page-locked host buffers ------------------

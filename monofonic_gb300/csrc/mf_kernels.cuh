@@ -420,7 +420,8 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
 #pragma unroll
       for (int s = 0; s < E; ++s) v[s] = src[FF::in_index(t, s)];
     }
-    for (int op = 0; op < nop && MODE != 2; ++op) {
+    const int nops = (MODE == 0) ? nop : (MODE == 1 ? 1 : 0);  // compile-time for the one-transform modes
+    for (int op = 0; op < nops; ++op) {
       const C* src = stage + (st * nop + op) * per_op + ly * kin;
 #pragma unroll
       for (int s = 0; s < E; ++s) v[s] = c2r_pre_s<T, H>(src, FI::in_index(t, s), kin, twM);
