@@ -141,16 +141,15 @@ def algorithmic_bytes_ic(n: int, prec_bytes: int, overload: int = 2, plt: bool =
         "conv_z": 27 * (S_MMK + S_R),
         "conv_yfwd": 10 * (S_MMK + S_MNK),
         "conv_xfwd": 10 * (S_MNK + S_NK),
-        # noise r2c z pass + per sub-lattice and pass three component c2r z passes
-        "fft_z": (1 + 2 * overload * 3) * 2 * S_N,
+        # noise r2c z pass + per sub-lattice and pass the three components' c2r z
+        # passes with the lattice readout fused (AoS positions / velocities out)
+        "fft_z": 2 * S_N + 2 * overload * (3 * S_N + 3 * n ** 3 * prec_bytes),
         # noise r2c y/x passes, three-component assembly x passes (order sum, A3 x3,
         # PLT table of 4 reals per mode, three outputs), component y passes
         "fft_col": 2 * 2 * S_NK + 2 * overload * ((1 + 3 + 3) * S_NK + (2 * S_NK if plt else 0))
                    + 2 * overload * 3 * 2 * S_NK,
-        # source products (7 + 10 + 21 real fields), two FP64 order sums (3 in, 1 out),
-        # lattice readout (3 component grids in, AoS positions/velocities out), ids
-        "pointwise": (7 + 10 + 21) * S_R + 2 * 4 * S_NK
-                     + 2 * overload * 3 * S_N + 2 * npart * 3 * prec_bytes + npart * 8,
+        # source products (7 + 10 + 21 real fields), two FP64 order sums (3 in, 1 out), ids
+        "pointwise": (7 + 10 + 21) * S_R + 2 * 4 * S_NK + npart * 8,
     }
     return out
 

@@ -645,13 +645,28 @@ int enqueue_impl(mf_ic* ic) {
           LaunchScope ls(c, KK_FFT_COL);
           CK(Launch<T>::colfft_plain(n, true, PlainStridedOp<T>{tk, Kz, (long long)n * Kz, T(1)}, n, Kz, twN, s));
         }
-        {
+        if (!three) {
           LaunchScope ls(c, KK_FFT_Z);
           const T norm = T(1.0 / std::sqrt((double)n * (double)n * (double)n));
           CK(Launch<T>::z_c2r_plain(n / 2, PlainZOp<T>{tmpr, n, norm}, n * n, Kz, twH, twN, s));
         }
       }
       const double* qt = ic->qtab + (size_t)ish * 3 * n;
+      if (three) {  // the three components' z passes with the lattice readout fused
+        Lattice3Args la{};
+        for (int d = 0; d < 3; ++d) la.comp[d] = ic->tmp[d]->d;
+        la.dst = dst;
+        la.q = qt;
+        la.n = n;
+        la.nlines = n * n;
+        la.ishift = fields ? 0 : ish;
+        la.with_q = (!fields && !vel) ? 1 : 0;
+        la.fields_mode = fields ? 1 : 0;
+        la.norm = 1.0 / std::sqrt((double)n * (double)n * (double)n);
+        LaunchScope ls(c, KK_FFT_Z);
+        CK(Launch<T>::z_c2r3_lattice(n / 2, la, fields || p.pos64, twH, twN, s));
+        continue;
+      }
       const T* q0 = (const T*)ic->tmp[0]->d;
       const T* q1 = (const T*)ic->tmp[1]->d;
       const T* q2 = (const T*)ic->tmp[2]->d;

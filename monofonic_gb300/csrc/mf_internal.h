@@ -58,6 +58,10 @@ struct Launch {
   static bool assemble3_supported(int L);
   static cudaError_t assemble3_xinv(int L, Assemble3XInvOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                     cudaStream_t s);
+  // z c2r of the three components with the lattice readout fused (H = n/2);
+  // p64: double positions / velocities (and fields mode)
+  static cudaError_t z_c2r3_lattice(int H, const Lattice3Args& a, bool p64, const cplx<T>* twH, const cplx<T>* twM,
+                                    cudaStream_t s);
   static cudaError_t conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
                                const cplx<T>* tw, cudaStream_t s);
   static cudaError_t conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,

@@ -257,6 +257,71 @@ __global__ void __launch_bounds__(NT) k_zc2r(OP op, const cplx<T>* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// z pass c2r of the three displacement / velocity components of a line, with
+// the lattice readout fused (set_positions / set_velocities,
+// particle_generator.hh:499-639): particle ip = ishift*n^3 + cell, AoS
+// [ip][3] of q + Psi (FP64 sum, stored as P) or, in fields mode, three n^3
+// grids of doubles.  Inputs: the three component grids after their x and y
+// passes, [line][n/2+1] complex.
+// ---------------------------------------------------------------------------
+template <typename T, int H, int NT, typename P>
+__global__ void __launch_bounds__(NT) k_zc2r3_lattice(Lattice3Args a, const cplx<T>* __restrict__ twH,
+                                                       const cplx<T>* __restrict__ twM) {
+  using F = LineFFT<T, H, true>;
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int t = threadIdx.x, ly = threadIdx.y;
+  const int line = blockIdx.x * blockDim.y + ly;
+  const bool valid = line < a.nlines;
+  const int n = a.n, Kz = H + 1;
+  C* sm[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    sm[d] = reinterpret_cast<C*>(smem_raw) + (ly * 3 + d) * (H + 1);
+    const C* src = reinterpret_cast<const C*>(a.comp[d]) + (long long)(valid ? line : 0) * Kz;
+    for (int k = t; k <= H; k += F::TPL) sm[d][k] = valid ? src[k] : mkc<T>(T(0), T(0));
+  }
+  __syncthreads();
+  C v[3][F::E];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) v[d][s] = c2r_pre<T, H>(sm[d], F::in_index(t, s), twM);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) F::run(v[d], t, sm[d], 1, twH, SyncBlock{});
+  if (!valid) return;
+  const long long n3 = (long long)n * n * n;
+  const int i = line / n, j = line % n;
+#pragma unroll
+  for (int s = 0; s < F::E; ++s) {
+    const int m = F::out_index(t, s);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 2 * m + h;
+      const long long c = (long long)line * n + k;
+      double val[3];
+      // normalised in the grid precision, as the component grids of the per-component path
+#pragma unroll
+      for (int d = 0; d < 3; ++d) val[d] = (double)((h ? v[d][s].y : v[d][s].x) * T(a.norm));
+      if (a.fields_mode) {
+        double* o = reinterpret_cast<double*>(a.dst);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[d * n3 + c] = val[d];
+      } else {
+        if (a.with_q) {
+          val[0] += a.q[i];
+          val[1] += a.q[n + j];
+          val[2] += a.q[2 * n + k];
+        }
+        P* o = reinterpret_cast<P*>(a.dst) + 3 * ((long long)a.ishift * n3 + c);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[d] = (P)val[d];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // fused Orszag z pass: per line, c2r of nop operands, pointwise product of
 // the real values, r2c of the product, store of kz in [0, kout)
 // ---------------------------------------------------------------------------

@@ -278,6 +278,34 @@ cudaError_t Launch<T>::assemble3_xinv(int L, Assemble3XInvOp<T> op, int nslab, i
   switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T, int H>
+cudaError_t launch_zc2r3_lattice(const Lattice3Args& a, bool p64, const cplx<T>* twH, const cplx<T>* twM,
+                                 cudaStream_t s) {
+  constexpr int LPB = z_lpb<T, H, 3 * (H + 1)>();
+  constexpr int TPL = LineFFT<T, H, true>::TPL;
+  const size_t smem = (size_t)LPB * 3 * (H + 1) * sizeof(cplx<T>);
+  dim3 block(TPL, LPB), grid((a.nlines + LPB - 1) / LPB);
+  if (p64) {
+    auto kern = k_zc2r3_lattice<T, H, TPL * LPB, double>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, block, smem, s>>>(a, twH, twM);
+  } else {
+    auto kern = k_zc2r3_lattice<T, H, TPL * LPB, float>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, block, smem, s>>>(a, twH, twM);
+  }
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t Launch<T>::z_c2r3_lattice(int H, const Lattice3Args& a, bool p64, const cplx<T>* twH,
+                                      const cplx<T>* twM, cudaStream_t s) {
+#define CASE(HH) case HH: return launch_zc2r3_lattice<T, HH>(a, p64, twH, twM, s);
+  switch (H) { MF_LEN_NH(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
+template cudaError_t Launch<MF_T>::z_c2r3_lattice(int, const Lattice3Args&, bool, const cplx<MF_T>*, const cplx<MF_T>*, cudaStream_t);
 template bool Launch<MF_T>::assemble3_supported(int);
 template cudaError_t Launch<MF_T>::assemble3_xinv(int, Assemble3XInvOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::colfft_plain(int, bool, PlainStridedOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);

@@ -527,6 +527,15 @@ struct Assemble3XInvOp {
   }
 };
 
+// arguments of the fused z c2r + lattice readout (mf_kernels.cuh, k_zc2r3_lattice)
+struct Lattice3Args {
+  const void* comp[3];
+  void* dst;
+  const double* q;  // q[d*n + idx_d], lattice coordinates times the unit
+  int n, nlines, ishift, with_q, fields_mode;
+  double norm;      // 1/sqrt(n^3) of the c2r
+};
+
 // z pass c2r of a work-buffer line [line][Kz] (kz > N/2 zero) into a real line
 template <typename T>
 struct PadC2RZOp {
