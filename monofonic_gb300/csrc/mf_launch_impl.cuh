@@ -18,6 +18,10 @@
 #ifndef MF_ZCONV_TMA
 #define MF_ZCONV_TMA 1
 #endif
+// divisor of the lines per batch of the one-transform TMA z passes (a build-time knob)
+#ifndef MF_ZONE_LPB_DIV
+#define MF_ZONE_LPB_DIV 1
+#endif
 // largest radix of the TMA z pass plan (8: fewer exchanges, more registers)
 #ifndef MF_ZCONV_TMA_MAXR
 #define MF_ZCONV_TMA_MAXR 8
@@ -56,13 +60,17 @@ inline cudaError_t set_smem(K kern, size_t smem) {
   return cudaSuccess;
 }
 
-// columns per CTA of the pipelined strided pass (two tile buffers): 64-byte
-// rows, at least 128 threads
+// row bytes of a tile of the pipelined strided pass (a build-time knob)
+#ifndef MF_PIPE_ROW_BYTES
+#define MF_PIPE_ROW_BYTES 64
+#endif
+// columns per CTA of the pipelined strided pass (two tile buffers): rows of
+// MF_PIPE_ROW_BYTES while both buffers fit in 220 KB, at least 128 threads
 template <typename T, int L>
 constexpr int pipe_ncol() {
   constexpr int tpl = LineFFT<T, L, false>::TPL;
-  int nc = (sizeof(T) == 4) ? 8 : 4;
-  while (nc * tpl > 1024) nc /= 2;
+  int nc = MF_PIPE_ROW_BYTES / (int)(2 * sizeof(T));
+  while (nc > 1 && (nc * tpl > 1024 || 2 * L * nc * (int)(2 * sizeof(T)) > 220 * 1024)) nc /= 2;
   while (nc * tpl < 128 && nc < 32) nc *= 2;
   return nc;
 }
@@ -157,7 +165,10 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
     constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
     using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
-    constexpr int LPBT = tma_lines_per_batch<T, TPL>();
+    // lines per batch; the one-transform modes may use a fraction of it (a
+    // build-time knob: more, smaller CTAs per SM)
+    constexpr int LPB0 = tma_lines_per_batch<T, TPL>();
+    constexpr int LPBT = (MODE != 0 && LPB0 >= 2 * MF_ZONE_LPB_DIV) ? LPB0 / MF_ZONE_LPB_DIV : LPB0;
     const bool tma_ok = MF_ZCONV_TMA && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
                         (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
@@ -173,7 +184,8 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, LPBT * TPL, smem);
       if (e != cudaSuccess) return e;
-      if (sc.occ > 0 && sc.occ < per_sm) per_sm = sc.occ;
+      // the autotuned CTAs per SM belong to the fused convolution pass (MODE 0)
+      if (MODE == 0 && sc.occ > 0 && sc.occ < per_sm) per_sm = sc.occ;
       if (per_sm < 1) per_sm = 1;
       const int nbatch = a.nlines / LPBT;
       int grid = nsm * per_sm;
