@@ -299,6 +299,13 @@ __global__ void __launch_bounds__(NT) k_zc2r3_lattice(Lattice3Args a, const cplx
     for (int h = 0; h < 2; ++h) {
       const int k = 2 * m + h;
       const long long c = (long long)line * n + k;
+      if (std::is_same<P, T>::value && !a.with_q && !a.fields_mode) {
+        // velocities (no lattice coordinate) in the grid precision: no FP64 step
+        P* o = reinterpret_cast<P*>(a.dst) + 3 * ((long long)a.ishift * n3 + c);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[d] = (P)((h ? v[d][s].y : v[d][s].x) * T(a.norm));
+        continue;
+      }
       double val[3];
       // normalised in the grid precision, as the component grids of the per-component path
 #pragma unroll
