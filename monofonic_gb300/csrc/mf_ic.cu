@@ -15,6 +15,13 @@
 #include "mf_plt.h"
 #include "mf_runtime.h"
 
+// host hand-off during a run (a build-time knob): 0 copies the positions
+// while the velocities are assembled; 1 streams the IDs and every
+// sub-lattice slice as soon as each is final
+#ifndef MF_STREAM_HANDOFF
+#define MF_STREAM_HANDOFF 0
+#endif
+
 namespace mf {
 namespace {
 
@@ -192,7 +199,8 @@ struct mf_ic {
   cudaStream_t cstream = nullptr;
   cudaEvent_t ev_pos = nullptr, ev_copy = nullptr;
   const mf_particles* early = nullptr;
-  bool pos_copied = false;
+  bool early_all = false;  // every particle array was streamed to the host during the run
+  bool pos_early = false;  // the positions were copied during the run
   // shared-source convolutions: padded real fields and three work buffers
   bool shared = false;
   void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last 5 or 1: product sums)
@@ -460,6 +468,28 @@ int enqueue_impl(mf_ic* ic) {
 
   if (timed) CK(cudaEventRecord(ic->ev[0], s));
   CK(cudaMemcpyAsync(ic->dyn_d, ic->dyn_h, sizeof(ICDyn), cudaMemcpyHostToDevice, s));
+  const bool fields = p.out_kind == MF_OUT_FIELDS;
+  const int overload = 1 << p.lattice;
+  // host hand-off during the run: each particle array (or sub-lattice slice)
+  // is copied on the copy stream as soon as it is final
+  auto early_copy = [&](void* hdst, const void* dsrc, size_t bytes) -> cudaError_t {
+    cudaError_t e2 = cudaEventRecord(ic->ev_pos, s);
+    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(ic->cstream, ic->ev_pos, 0);
+    if (e2 == cudaSuccess) e2 = cudaMemcpyAsync(hdst, dsrc, bytes, cudaMemcpyDeviceToHost, ic->cstream);
+    if (e2 == cudaSuccess) e2 = cudaEventRecord(ic->ev_copy, ic->cstream);
+    return e2;
+  };
+  // ---- particle IDs (particle_generator.hh:212-253): independent of the
+  // fields, so they are made first and their copy overlaps the whole run
+  if (!fields) {
+    LaunchScope ls(c, KK_POINTWISE);
+    if (p.id64)
+      k_ids<uint64_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint64_t*)ic->dids, n, overload, 0);
+    else
+      k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->dids, n, overload, 0);
+    CK(cudaGetLastError());
+    if (ic->early && MF_STREAM_HANDOFF) CK(early_copy(ic->early->ids, ic->dids, ic->id_bytes));
+  }
   // ---- white noise (RNG_plugin::Fill_Grid) to k-space, phi(1) -----------------
   if (ic->noise_seeded) {
     LaunchScope ls(c, KK_POINTWISE);
@@ -559,8 +589,6 @@ int enqueue_impl(mf_ic* ic) {
   }
   if (timed) CK(cudaEventRecord(ic->ev[4], s));
 
-  const int overload = 1 << p.lattice;
-  const bool fields = p.out_kind == MF_OUT_FIELDS;
   T* wsum = (T*)ic->wn->d;  // the noise grid is free after phi(1): holds the order sum
   const cplx<T>* P1 = (const cplx<T>*)ic->f[0]->d;
   const cplx<T>* P2 = ic->f[1] ? (const cplx<T>*)ic->f[1]->d : nullptr;
@@ -663,8 +691,15 @@ int enqueue_impl(mf_ic* ic) {
         la.with_q = (!fields && !vel) ? 1 : 0;
         la.fields_mode = fields ? 1 : 0;
         la.norm = 1.0 / std::sqrt((double)n * (double)n * (double)n);
-        LaunchScope ls(c, KK_FFT_Z);
-        CK(Launch<T>::z_c2r3_lattice(n / 2, la, fields || p.pos64, twH, twN, s));
+        {
+          LaunchScope ls(c, KK_FFT_Z);
+          CK(Launch<T>::z_c2r3_lattice(n / 2, la, fields || p.pos64, twH, twN, s));
+        }
+        if (ic->early && !fields && MF_STREAM_HANDOFF) {
+          const size_t slice = (vel ? ic->vel_bytes : ic->pos_bytes) / overload;
+          CK(early_copy((char*)(vel ? ic->early->vel : ic->early->pos) + ish * slice, (const char*)dst + ish * slice,
+                        slice));
+        }
         continue;
       }
       const T* q0 = (const T*)ic->tmp[0]->d;
@@ -678,26 +713,20 @@ int enqueue_impl(mf_ic* ic) {
       else
         k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, qt, vel ? 0 : 1, 0);
       CK(cudaGetLastError());
+      if (ic->early && !fields && MF_STREAM_HANDOFF) {
+        const size_t slice = (vel ? ic->vel_bytes : ic->pos_bytes) / overload;
+        CK(early_copy((char*)(vel ? ic->early->vel : ic->early->pos) + ish * slice, (const char*)dst + ish * slice,
+                      slice));
+      }
     }
     if (timed) CK(cudaEventRecord(ic->ev[5 + pass], s));
-    if (pass == 0 && ic->early) {  // positions are final: start their copy to the host
-      CK(cudaEventRecord(ic->ev_pos, s));
-      CK(cudaStreamWaitEvent(ic->cstream, ic->ev_pos, 0));
-      CK(cudaMemcpyAsync(ic->early->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, ic->cstream));
-      CK(cudaEventRecord(ic->ev_copy, ic->cstream));
-      ic->pos_copied = true;
-    }
+    if (ic->early && (fields || !MF_STREAM_HANDOFF) && !vel)  // positions final: copy them during the velocity pass
+      CK(early_copy(ic->early->pos, dst, ic->pos_bytes));
+    if (ic->early && fields && MF_STREAM_HANDOFF && vel) CK(early_copy(ic->early->vel, dst, ic->vel_bytes));
   }
-  // ---- particle IDs (particle_generator.hh:212-253) ------------------------
-  if (!fields) {
-    LaunchScope ls(c, KK_POINTWISE);
-    if (p.id64)
-      k_ids<uint64_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint64_t*)ic->dids, n, overload, 0);
-    else
-      k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->dids, n, overload, 0);
-    CK(cudaGetLastError());
-  }
-  if (timed) CK(cudaEventRecord(ic->ev[7], s));
+  if (timed) CK(cudaEventRecord(ic->ev[7], s));  // (the IDs are made at the start)
+  if (ic->early) ic->early_all = MF_STREAM_HANDOFF;
+  if (ic->early) ic->pos_early = true;
 #undef CK
   return MF_OK;
 }
@@ -717,10 +746,12 @@ int handoff(mf_ic* ic, mf_particles* out) {
     out->npart = ic->npart;
     if (out->location == MF_LOC_HOST) {
       if (!out->pos || !out->vel || (!fields && !out->ids)) return set_err(c, MF_ERR_ARG, "mf_ic_run: null host buffer");
-      if (!ic->pos_copied) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
-      CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, s));
-      if (!fields) CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, s));
-      if (ic->pos_copied) CK(cudaStreamWaitEvent(s, ic->ev_copy, 0));  // the run ends after both copies
+      if (!ic->early_all) {
+        if (!ic->pos_early) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, s));
+        if (!fields) CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, s));
+      }
+      if (ic->pos_early) CK(cudaStreamWaitEvent(s, ic->ev_copy, 0));  // the run ends after the streamed copies
     } else {
       out->pos = ic->dpos;
       out->vel = ic->dvel;
@@ -1016,8 +1047,10 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
   if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
   ic->early = nullptr;
-  ic->pos_copied = false;
-  if (out && out->location == MF_LOC_HOST && out->pos && out->vel) {
+  ic->early_all = false;
+  ic->pos_early = false;
+  if (out && out->location == MF_LOC_HOST && out->pos && out->vel &&
+      (ic->p.out_kind == MF_OUT_FIELDS || out->ids)) {
     cudaError_t e = cudaSuccess;
     if (!ic->cstream) e = cudaStreamCreateWithFlags(&ic->cstream, cudaStreamNonBlocking);
     if (e == cudaSuccess && !ic->ev_pos) e = cudaEventCreateWithFlags(&ic->ev_pos, cudaEventDisableTiming);
@@ -1031,7 +1064,8 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   else cudaStreamSynchronize(ic->ctx->stream);
   if (ic->cstream) cudaStreamSynchronize(ic->cstream);
   ic->early = nullptr;
-  ic->pos_copied = false;
+  ic->early_all = false;
+  ic->pos_early = false;
   return rc;
 }
 
