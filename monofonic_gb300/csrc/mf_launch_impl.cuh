@@ -20,7 +20,7 @@
 #endif
 // divisor of the lines per batch of the one-transform TMA z passes (a build-time knob)
 #ifndef MF_ZONE_LPB_DIV
-#define MF_ZONE_LPB_DIV 1
+#define MF_ZONE_LPB_DIV 2
 #endif
 // largest radix of the TMA z pass plan (8: fewer exchanges, more registers)
 #ifndef MF_ZCONV_TMA_MAXR
