@@ -187,6 +187,10 @@ __host__ __device__ constexpr FFTPlan make_plan(int L, int maxr) {
     while (rem > 0) { const int t = (rem >= 2) ? 2 : 1; rem -= t; p.r[p.n++] = 1 << t; }
   } else {
     while (a > 0) { const int t = (a >= 2 && maxr >= 4) ? 2 : 1; a -= t; p.r[p.n++] = 1 << t; }
+    if (MF_FFT_COMPOSITE && maxr >= 4 && b > 0 && p.n > 0 && p.r[p.n - 1] <= 4) {
+      p.r[p.n - 1] *= 3;  // the last factor 4 or 2 merged with a factor 3 (radix 12 or 6)
+      --b;
+    }
   }
   for (int i = 0; i < b; ++i) p.r[p.n++] = 3;
   return p;

@@ -18,6 +18,11 @@
 #include "mf_fft.cuh"
 #include "mf_tma.cuh"
 
+// largest radix of the pipelined strided passes' plans (a build-time knob)
+#ifndef MF_COL_MAXR
+#define MF_COL_MAXR 8
+#endif
+
 namespace mf {
 
 // ops with a per-tile prologue (tile_prep / xform_tile) in the pipelined pass
@@ -111,9 +116,10 @@ k_colfft3(OP op, const cplx<T>* __restrict__ tw, int ncols) {
 //     (+ kPrefetch: prefetch/store_pre on the same coordinates)
 // ---------------------------------------------------------------------------
 template <typename T, int L, bool INV, int NCOL, class OP>
-__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV>::TPL, (NCOL * LineFFT<T, L, INV>::TPL <= 256) ? 2 : 1)
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
+                                  (NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL <= 256) ? 2 : 1)
 k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
-  using F = LineFFT<T, L, INV>;
+  using F = LineFFT<T, L, INV, MF_COL_MAXR>;
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf0 = reinterpret_cast<C*>(smem_raw);

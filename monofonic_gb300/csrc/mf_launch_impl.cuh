@@ -68,7 +68,7 @@ inline cudaError_t set_smem(K kern, size_t smem) {
 // MF_PIPE_ROW_BYTES while both buffers fit in 220 KB, at least 128 threads
 template <typename T, int L>
 constexpr int pipe_ncol() {
-  constexpr int tpl = LineFFT<T, L, false>::TPL;
+  constexpr int tpl = LineFFT<T, L, false, MF_COL_MAXR>::TPL;
   int nc = MF_PIPE_ROW_BYTES / (int)(2 * sizeof(T));
   while (nc > 1 && (nc * tpl > 1024 || 2 * L * nc * (int)(2 * sizeof(T)) > 220 * 1024)) nc /= 2;
   while (nc * tpl < 128 && nc < 32) nc *= 2;
@@ -79,7 +79,7 @@ template <typename T, int L, bool INV, class OP>
 cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s, int kind) {
   if constexpr (OP::kPipe && MF_COL_PIPE) {
     constexpr int NC = pipe_ncol<T, L>();
-    constexpr int TPL = LineFFT<T, L, INV>::TPL;
+    constexpr int TPL = LineFFT<T, L, INV, MF_COL_MAXR>::TPL;
     const size_t smem = (size_t)2 * L * NC * sizeof(cplx<T>);
     auto kern = k_colfft_pipe<T, L, INV, NC, OP>;
     cudaError_t e = set_smem(kern, smem);
