@@ -30,7 +30,8 @@ enum {
   MF_ERR_CUDA = 4,      /* a CUDA call failed */
   MF_ERR_TIMEOUT = 5,   /* a bounded wait ran out */
   MF_ERR_CANCELLED = 6, /* request cancelled */
-  MF_ERR_STATE = 7      /* object in the wrong state for the call */
+  MF_ERR_STATE = 7,     /* object in the wrong state for the call */
+  MF_ERR_IO = 8         /* a file could not be created or written */
 };
 
 /* arithmetic of a grid: plain FP64, or the FP32-bulk form */

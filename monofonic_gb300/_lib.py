@@ -12,7 +12,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libmfgpu.so")
 
-MF_OK, MF_ERR_ARG, MF_ERR_SHAPE, MF_ERR_OOM, MF_ERR_CUDA, MF_ERR_TIMEOUT, MF_ERR_CANCELLED, MF_ERR_STATE = range(8)
+MF_OK, MF_ERR_ARG, MF_ERR_SHAPE, MF_ERR_OOM, MF_ERR_CUDA, MF_ERR_TIMEOUT, MF_ERR_CANCELLED, MF_ERR_STATE, MF_ERR_IO = range(9)
 MF_PREC_F64, MF_PREC_F32 = 0, 1
 MF_SPACE_R, MF_SPACE_K = 0, 1
 MF_CONV_ORSZAG, MF_CONV_NAIVE = 0, 1
@@ -20,7 +20,8 @@ MF_OPND_PLAIN, MF_OPND_HESS, MF_OPND_SUM, MF_OPND_DIFF, MF_OPND_GRAD = range(5)
 MF_OP_ASSIGN, MF_OP_ADD, MF_OP_SUB, MF_OP_AXPY = range(4)
 
 ERROR_NAMES = {1: "MF_ERR_ARG", 2: "MF_ERR_SHAPE", 3: "MF_ERR_OOM", 4: "MF_ERR_CUDA",
-               5: "MF_ERR_TIMEOUT", 6: "MF_ERR_CANCELLED", 7: "MF_ERR_STATE"}
+               5: "MF_ERR_TIMEOUT", 6: "MF_ERR_CANCELLED", 7: "MF_ERR_STATE",
+               8: "MF_ERR_IO"}
 
 
 class mf_operand(C.Structure):
@@ -172,6 +173,30 @@ SIGNATURES.update({
     "mf_server_now": (C.c_double, [C.c_void_p]),
     "mf_server_last_error": (C.c_char_p, [C.c_void_p]),
     "mf_server_destroy": (C.c_int, [C.c_void_p]),
+})
+
+
+
+class mf_grafic2_params(C.Structure):
+    _fields_ = [("dirname", C.c_char_p), ("ngrid", C.c_int), ("boxlen", C.c_double), ("zstart", C.c_double),
+                ("H0", C.c_double), ("Omega_m", C.c_double), ("Omega_DE", C.c_double), ("Omega_b", C.c_double),
+                ("baryons", C.c_int), ("ramses_nml", C.c_int), ("use_spt", C.c_int), ("chunk_planes", C.c_int)]
+
+
+MF_FC_DENSITY, MF_FC_VX, MF_FC_VY, MF_FC_VZ, MF_FC_DX, MF_FC_DY, MF_FC_DZ, MF_FC_MASS = range(8)
+MF_SPECIES_DM, MF_SPECIES_BARYON, MF_SPECIES_NEUTRINO = range(3)
+MF_OUTTYPE_PARTICLES, MF_OUTTYPE_FIELD_LAGRANGIAN, MF_OUTTYPE_FIELD_EULERIAN = range(3)
+
+SIGNATURES.update({
+    "mf_grafic2_create": (C.c_int, [C.c_void_p, C.POINTER(mf_grafic2_params), C.POINTER(C.c_void_p)]),
+    "mf_grafic2_destroy": (C.c_int, [C.c_void_p]),
+    "mf_grafic2_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mf_grafic2_write_grid": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "mf_grafic2_write_field": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "mf_ic_write_grafic2": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mf_grafic2_last_write": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]),
 })
 
 _lib = None

@@ -1079,6 +1079,10 @@ extern "C" int mf_ic_particles(mf_ic* ic, mf_particles* out) {
   return MF_OK;
 }
 
+namespace mf {
+const mf_ic_params* ic_params(const mf_ic* ic) { return &ic->p; }
+}  // namespace mf
+
 extern "C" int mf_ic_context(mf_ic* ic, mf_ctx** out) {
   if (!ic || !out) return MF_ERR_ARG;
   *out = ic->ctx;
