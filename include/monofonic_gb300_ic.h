@@ -64,6 +64,8 @@ int mf_grid_fill_white_noise(mf_grid* g, uint64_t seed);
 
 /* ---- LPT pipeline (src/ic_generator.cc:90-948) -------------------------- */
 enum { MF_OUT_PARTICLES = 0, MF_OUT_FIELDS = 1 };
+/* include/general.hh:71-76 (enum class cosmo_species) */
+enum { MF_SPECIES_DM = 0, MF_SPECIES_BARYON, MF_SPECIES_NEUTRINO };
 enum { MF_LOC_HOST = 0, MF_LOC_DEVICE = 1 };
 
 typedef struct {
@@ -89,6 +91,17 @@ typedef struct {
                              real fields (each operand transformed once);
                              1: one convolution per term as the reference
                              orders them (less device memory) */
+  /* two-species ICs (ic_generator.cc:153-166, :608-792): dark matter on the
+   * lattice, baryons on the secondary lattice, perturbed particle masses */
+  int baryons;            /* setup/DoBaryons (particle output only)          */
+  int baryon_vrel;        /* setup/DoBaryonVrel: back-scaled decaying relative
+                             velocity mode                                  */
+  double munit;           /* output_plugin::mass_unit                       */
+  const double* tk_dbc_table; /* optional host tables T_delta_bc(k) and      */
+  const double* tk_tbc_table; /* T_theta_bc(k) at k = sqrt(k2)*2pi/L, k2 =
+                             0..3(n/2)^2; NULL: zero, as the Eisenstein-Hu
+                             plugin returns (transfer_eisenstein.cc:238-240) */
+  double Dplus_target;    /* D+ at cosmology/ztarget; 0: 1 (ztarget = 0)     */
 } mf_ic_params;
 
 /* Particle container (include/particle_container.hh:29-139): positions and
@@ -101,6 +114,8 @@ typedef struct {
   void* ids;
   int64_t npart;
   int location;       /* MF_LOC_HOST or MF_LOC_DEVICE */
+  void* mass;         /* per-particle masses (float or double as pos) of a
+                         two-species pipeline; unused otherwise          */
 } mf_particles;
 
 /* number of particles and output bytes for a parameter set */
@@ -138,6 +153,14 @@ int mf_ic_run(mf_ic* ic, mf_particles* out);
 int mf_ic_enqueue(mf_ic* ic);
 /* device buffers of the particles (location MF_LOC_DEVICE) */
 int mf_ic_particles(mf_ic* ic, mf_particles* out);
+/* two-species pipelines (p.baryons): run and hand over out[0] = dark matter,
+ * out[1] = baryons (nspecies = 2; each as mf_ic_run's out, with masses);
+ * mf_ic_run refuses such a pipeline */
+int mf_ic_run_species(mf_ic* ic, mf_particles* out, int nspecies);
+/* device buffers of one species (MF_SPECIES_DM = 0, MF_SPECIES_BARYON = 1) */
+int mf_ic_particles_species(mf_ic* ic, int species, mf_particles* out);
+/* bytes of one species' masses (0 without baryons) */
+int mf_ic_mass_bytes(const mf_ic_params* p, size_t* bytes);
 /* the context (and so the stream) the pipeline runs on */
 int mf_ic_context(mf_ic* ic, mf_ctx** out);
 /* per-stage device times of the last run in milliseconds:

@@ -26,11 +26,11 @@
 extern "C" {
 #endif
 
-/* include/general.hh:60-76 (enum class fluid_component / cosmo_species) */
+/* include/general.hh:60-70 (enum class fluid_component); the species enum
+ * is in monofonic_gb300_ic.h */
 enum {
   MF_FC_DENSITY = 0, MF_FC_VX, MF_FC_VY, MF_FC_VZ, MF_FC_DX, MF_FC_DY, MF_FC_DZ, MF_FC_MASS
 };
-enum { MF_SPECIES_DM = 0, MF_SPECIES_BARYON, MF_SPECIES_NEUTRINO };
 /* include/output_plugin.hh:30 (enum class output_type) */
 enum { MF_OUTTYPE_PARTICLES = 0, MF_OUTTYPE_FIELD_LAGRANGIAN, MF_OUTTYPE_FIELD_EULERIAN };
 

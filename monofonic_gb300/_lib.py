@@ -89,12 +89,13 @@ class mf_ic_params(C.Structure):
                 ("inversion", C.c_int), ("plt", C.c_int), ("cosmo", mf_cosmo_scalars),
                 ("tk_table", C.c_void_p), ("lunit", C.c_double), ("vunit", C.c_double), ("out_kind", C.c_int),
                 ("pos64", C.c_int), ("id64", C.c_int), ("plt_ngrid", C.c_int),
-                ("per_term_conv", C.c_int)]
+                ("per_term_conv", C.c_int), ("baryons", C.c_int), ("baryon_vrel", C.c_int), ("munit", C.c_double),
+                ("tk_dbc_table", C.c_void_p), ("tk_tbc_table", C.c_void_p), ("Dplus_target", C.c_double)]
 
 
 class mf_particles(C.Structure):
     _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("ids", C.c_void_p), ("npart", C.c_int64),
-                ("location", C.c_int)]
+                ("location", C.c_int), ("mass", C.c_void_p)]
 
 
 MF_OUT_PARTICLES, MF_OUT_FIELDS = 0, 1
@@ -122,6 +123,9 @@ SIGNATURES.update({
     "mf_ic_set_cosmology": (C.c_int, [C.c_void_p, C.POINTER(mf_cosmo_scalars)]),
     "mf_ic_enqueue": (C.c_int, [C.c_void_p]),
     "mf_ic_particles": (C.c_int, [C.c_void_p, C.POINTER(mf_particles)]),
+    "mf_ic_run_species": (C.c_int, [C.c_void_p, C.POINTER(mf_particles), C.c_int]),
+    "mf_ic_particles_species": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(mf_particles)]),
+    "mf_ic_mass_bytes": (C.c_int, [C.POINTER(mf_ic_params), C.POINTER(C.c_size_t)]),
     "mf_ic_context": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
 })
 

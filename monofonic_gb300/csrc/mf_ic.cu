@@ -40,7 +40,90 @@ struct ICDyn {
   double half_ns, sqrtpnorm;
   double w[2][4];           // positions / velocities: weights of phi, phi2, phi3 and the A3 term
   unsigned long long seed;  // white-noise seed (device generator)
+  // two species (ic_generator.cc:157-166, :615-619): C_species, Omega_species,
+  // the theta_bc weight of the velocities (-vfac C_species, 0 without the
+  // relative-velocity mode), D+_target and sqrt(D+_target / D+_start)
+  double Cs[2], Omega_s[2], wbc[2];
+  double bc_Dt, bc_sqrtDr;
+  int vrel;
 };
+
+// amplitudes of the baryon-CDM modes per integer k^2: get_amplitude_delta_bc
+// and get_amplitude_theta_bc (cosmology_calculator.hh:416-431) from the host
+// tables of T_delta_bc and T_theta_bc (zero where a table is absent)
+__global__ void k_amp_bc(double* ampd, double* ampt, int nk2, double kfac, const ICDyn* __restrict__ dyn,
+                         const double* tdbc, const double* ttbc) {
+  const double half_ns = dyn->half_ns, sqrtpnorm = dyn->sqrtpnorm, Dt = dyn->bc_Dt, sDr = dyn->bc_sqrtDr;
+  const int vrel = dyn->vrel;
+  for (int k2 = blockIdx.x * blockDim.x + threadIdx.x; k2 < nk2; k2 += gridDim.x * blockDim.x) {
+    const double k = sqrt((double)k2) * kfac;
+    const double td = tdbc ? tdbc[k2] : 0.0, tt = ttbc ? ttbc[k2] : 0.0;
+    const double dbc = td + (vrel ? 2 * tt * (sDr - 1.0) : 0.0);
+    ampd[k2] = pow(k, half_ns) * dbc * (sqrtpnorm * Dt);
+    ampt[k2] = vrel ? pow(k, half_ns) * (tt * sDr) * (sqrtpnorm * Dt) : 0.0;
+  }
+}
+
+// baryon-CDM fields from the normalised noise: rho_bc = wn amp_dbc
+// (ic_generator.cc:655-660) and the relative-velocity potential
+// psi_bc = amp_tbc wn / k^2 (ic_generator.cc:907-910), both with zero DC
+template <typename T>
+__global__ void k_bc_fields(const cplx<T>* wn, cplx<T>* rho, cplx<T>* psi, int n, double kfac, const double* ampd,
+                            const double* ampt) {
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    const int ii = i - (i > n / 2 ? n : 0), jj = j - (j > n / 2 ? n : 0);
+    const int k2 = ii * ii + jj * jj + kz * kz;
+    const cplx<T> w = wn[idx];
+    if (rho) {
+      const T a = T(ampd[k2]);
+      rho[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(w.x * a, w.y * a);
+    }
+    if (psi) {
+      const T kx = T(ii) * T(kfac), ky = T(jj) * T(kfac), kk = T(kz) * T(kfac);
+      const T kn2 = kx * kx + ky * ky + kk * kk;
+      const T a = T(ampt[k2]);
+      psi[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(w.x * a / kn2, w.y * a / kn2);
+    }
+  }
+}
+
+// one shift_field chain over a k-space grid (set_masses, particle_generator.hh:389-401)
+template <typename T>
+__global__ void k_shift_chain(const cplx<T>* src, cplx<T>* dst, int n, ShiftChain<T> ch) {
+  const int Kz = n / 2 + 1;
+  const size_t tot = (size_t)n * n * Kz;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(idx % Kz);
+    const int j = (int)((idx / Kz) % n);
+    const int i = (int)(idx / ((size_t)Kz * n));
+    cplx<T> v[1] = {src[idx]};
+    cplx<T> vm[1] = {mkc<T>(T(0), T(0))};
+    if (kz == 0 || kz == n / 2) vm[0] = src[((size_t)((n - i) % n) * n + (n - j) % n) * Kz + kz];
+    ch.apply<1>(n, i, j, kz, v, vm);
+    dst[idx] = v[0];
+  }
+}
+
+// set_masses (particle_generator.hh:369-422): particle ip = ishift*n^3 + cell
+// gets pmeanmass * (1 + C_s delta_bc) Omega_s munit (ic_generator.cc:662-664),
+// delta_bc read from the shifted real field (padded rows), or 0
+template <typename T, typename P>
+__global__ void k_masses(P* mass, const T* delta, int n, int ishift, double pmean, double munit,
+                         const ICDyn* __restrict__ dyn, int species) {
+  const size_t n3 = (size_t)n * n * n;
+  const double C = dyn->Cs[species], Om = dyn->Omega_s[species];
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n3; c += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = c / ((size_t)n * n), j = (c / n) % n, k = c % n;
+    const double v = delta ? (double)delta[(i * n + j) * (n + 2) + k] : 0.0;
+    const double rho = (1.0 + C * v) * Om * munit;
+    mass[(size_t)ishift * n3 + c] = (P)(pmean * rho);
+  }
+}
 
 // amplitude table amp(k2) = k^{n_s/2} T(k) sqrt(pnorm), k = sqrt(k2)*kfac
 // (get_amplitude, include/cosmology_calculator.hh:405-408), FP64
@@ -85,13 +168,17 @@ __global__ void k_phi1(cplx<T>* wn, cplx<T>* phi, int n, double kfac, const doub
 // :835-845 / :889-899) in FP64, stored in the grid precision
 template <typename T>
 __global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, const cplx<T>* p3, size_t tot,
-                         const double* __restrict__ w) {
+                         const double* __restrict__ w, const cplx<T>* pbc = nullptr,
+                         const double* __restrict__ wbc = nullptr) {
   const double w1 = w[0], w2 = w[1], w3 = w[2];
+  const double wb = pbc ? *wbc : 0.0;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
     const cplx<T> a = p1[idx];
     double r = w1 * (double)a.x, im = w1 * (double)a.y;
     if (p2) { const cplx<T> b = p2[idx]; r += w2 * (double)b.x; im += w2 * (double)b.y; }
     if (p3) { const cplx<T> c = p3[idx]; r += w3 * (double)c.x; im += w3 * (double)c.y; }
+    // the relative-velocity term of a two-species run (ic_generator.cc:907-910)
+    if (pbc) { const cplx<T> b = pbc[idx]; r += wb * (double)b.x; im += wb * (double)b.y; }
     out[idx] = mkc<T>(T(r), T(im));
   }
 }
@@ -162,6 +249,26 @@ const double kShifts[4][8][3] = {
     {{0, 0, 0}, {0, 0.5, 0.5}, {0.5, 0, 0.5}, {0.5, 0.5, 0}},
     {{0, 0, 0}, {0, 0, 0.5}, {0, 0.5, 0}, {0, 0.5, 0.5}, {0.5, 0, 0}, {0.5, 0, 0.5}, {0.5, 0.5, 0}, {0.5, 0.5, 0.5}},
 };
+// shift of the secondary (baryon) lattice (particle_generator.hh:56-63)
+const double kSecondShift[4][3] = {{0.5, 0.5, 0.5}, {0.5, 0.5, 0.0}, {0.5, 0.5, 0.5}, {0.25, 0.25, 0.25}};
+
+// shift_field chain of sub-lattice ish (particle_generator.hh:389-401, :510-522,
+// :607-618): the secondary lattice's global shift first, then the relative
+// shifts of sub-lattices 1..ish, in quarter cells
+template <typename T>
+ShiftChain<T> lattice_chain(const void* phase, int lattice, bool secondary, int ish) {
+  ShiftChain<T> ch{};
+  ch.phase = (const cplx<T>*)phase;
+  ch.nstep = 0;
+  if (secondary) {
+    for (int q = 0; q < 3; ++q) ch.s4[0][q] = (int)lround(4 * kSecondShift[lattice][q]);
+    ch.nstep = 1;
+  }
+  for (int st = 1; st <= ish; ++st, ++ch.nstep)
+    for (int q = 0; q < 3; ++q)
+      ch.s4[ch.nstep][q] = (int)lround(4 * (kShifts[lattice][st][q] - kShifts[lattice][st - 1][q]));
+  return ch;
+}
 
 }  // namespace
 }  // namespace mf
@@ -174,7 +281,7 @@ struct mf_ic {
   mf_grid* wn = nullptr;
   mf_grid* f[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // phi, phi2, phi3, A3x, A3y, A3z
   mf_grid* tmp[3] = {nullptr, nullptr, nullptr};  // real-space components of one sub-lattice
-  void* phase = nullptr;  // exp(+2 pi i m / 2n), m in [0, 2n), grid precision
+  void* phase = nullptr;  // exp(+2 pi i m / 4n), m in [0, 4n), grid precision
   double* qtab = nullptr; // lattice coordinates q[ishift][d][idx] * lunit
   void* plt = nullptr;    // PLT tables Dr, Dth, Dph, Dvf in the grid precision
   void* pltg = nullptr;   // PLT gradient and vfac_corr per N-grid mode [idx][4]
@@ -187,6 +294,19 @@ struct mf_ic {
   void* dvel = nullptr;
   void* dids = nullptr;
   size_t pos_bytes = 0, vel_bytes = 0, id_bytes = 0;
+  // two species: the baryons' particle arrays, both species' masses, the
+  // baryon-CDM amplitude tables and fields
+  void* bpos = nullptr;
+  void* bvel = nullptr;
+  void* bids = nullptr;
+  void* dmass[2] = {nullptr, nullptr};
+  size_t mass_bytes = 0;
+  double* bqtab = nullptr;  // secondary-lattice coordinates, as qtab
+  double* ampbc = nullptr;  // [0, nk2) amp_dbc, [nk2, 2 nk2) amp_tbc, then the host tables
+  const double* tdbc_d = nullptr;
+  const double* ttbc_d = nullptr;
+  mf_grid* rho_bc = nullptr;  // k-space wn amp_dbc
+  mf_grid* psi_bc = nullptr;  // k-space amp_tbc wn / k^2
   int64_t npart = 0;
   cudaEvent_t ev[9] = {};
   bool noise_set = false;   // an uploaded white-noise field is waiting in wn
@@ -227,6 +347,12 @@ int check_params(const mf_ic_params* p) {
   if (p->out_kind == MF_OUT_FIELDS && p->lattice != MF_LATTICE_SC) return MF_ERR_ARG;
   if (!(p->boxlen > 0)) return MF_ERR_ARG;
   if (p->plt && p->plt_ngrid != 0 && !grid_size_supported(p->plt_ngrid)) return MF_ERR_SHAPE;
+  if (p->baryons) {
+    // two-species field output goes through the semiclassical Eulerian branch, not built
+    if (p->out_kind != MF_OUT_PARTICLES) return MF_ERR_ARG;
+    if (!(p->munit > 0) || !(p->cosmo.Omega_b > 0) || !(p->cosmo.Omega_m > p->cosmo.Omega_b)) return MF_ERR_ARG;
+    if (p->Dplus_target < 0) return MF_ERR_ARG;
+  }
   return MF_OK;
 }
 
@@ -261,6 +387,18 @@ void fill_dyn(mf_ic* ic) {
   const double g3c = (p.lpt_order > 2) ? 1.0 / 7.0 * D * D * D : 0.0;
   d.w[0][0] = g1; d.w[0][1] = g2; d.w[0][2] = g3; d.w[0][3] = g3c;
   d.w[1][0] = vf * g1; d.w[1][1] = 2 * vf * g2; d.w[1][2] = 3 * vf * g3; d.w[1][3] = 3 * vf * g3c;
+  if (p.baryons) {
+    const double Om = p.cosmo.Omega_m, Ob = p.cosmo.Omega_b, fb = Ob / Om;
+    d.Cs[0] = -fb;        // dark matter
+    d.Cs[1] = 1.0 - fb;   // baryons
+    d.Omega_s[0] = Om - Ob;
+    d.Omega_s[1] = Ob;
+    d.vrel = p.baryon_vrel ? 1 : 0;
+    d.wbc[0] = d.vrel ? -vf * d.Cs[0] : 0.0;
+    d.wbc[1] = d.vrel ? -vf * d.Cs[1] : 0.0;
+    d.bc_Dt = p.Dplus_target > 0 ? p.Dplus_target : 1.0;
+    d.bc_sqrtDr = std::sqrt(d.bc_Dt / D);
+  }
 }
 
 // phi(2), phi(3) and A(3) with shared padded real fields (ic_generator.cc:471-545).
@@ -489,6 +627,14 @@ int enqueue_impl(mf_ic* ic) {
       k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->dids, n, overload, 0);
     CK(cudaGetLastError());
     if (ic->early && MF_STREAM_HANDOFF) CK(early_copy(ic->early->ids, ic->dids, ic->id_bytes));
+    if (p.baryons) {  // baryon IDs start at IDoffset = 1 (ic_generator.cc:626-628)
+      const uint64_t off = (uint64_t)overload * n * n * n;
+      if (p.id64)
+        k_ids<uint64_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint64_t*)ic->bids, n, overload, off);
+      else
+        k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->bids, n, overload, off);
+      CK(cudaGetLastError());
+    }
   }
   // ---- white noise (RNG_plugin::Fill_Grid) to k-space, phi(1) -----------------
   if (ic->noise_seeded) {
@@ -509,6 +655,19 @@ int enqueue_impl(mf_ic* ic) {
                                                    p.fixing);
     CK(cudaGetLastError());
     ic->f[0]->space = MF_SPACE_K;
+  }
+  // ---- baryon-CDM fields of a two-species run, from the normalised noise
+  // before its grid is reused (ic_generator.cc:655-660, :907-910)
+  if (ic->rho_bc) {
+    LaunchScope ls(c, KK_POINTWISE);
+    double* ampd = ic->ampbc;
+    double* ampt = ic->ampbc + ic->nk2;
+    k_amp_bc<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ampd, ampt, ic->nk2, kfac, ic->dyn_d, ic->tdbc_d, ic->ttbc_d);
+    CK(cudaGetLastError());
+    k_bc_fields<T><<<blocks_for(nk), kThreads, 0, s>>>((const cplx<T>*)ic->wn->d, (cplx<T>*)ic->rho_bc->d,
+                                                        ic->psi_bc ? (cplx<T>*)ic->psi_bc->d : nullptr, n, kfac, ampd,
+                                                        ampt);
+    CK(cudaGetLastError());
   }
   if (timed) CK(cudaEventRecord(ic->ev[1], s));
 
@@ -597,15 +756,22 @@ int enqueue_impl(mf_ic* ic) {
   const cplx<T>* twH = c->tw.get<T>(n / 2, s);
   if (!twN || !twH) return set_err(c, MF_ERR_OOM, "twiddles");
   const size_t n3 = (size_t)n * n * n;
+  const int nsp = p.baryons ? 2 : 1;  // species: dark matter, then baryons on the secondary lattice
   for (int pass = 0; pass < 2; ++pass) {  // 0: positions, 1: velocities
     const bool vel = pass == 1;
-    {
+    for (int sp = 0; sp < nsp; ++sp) {
+    // the order sum is the same for both species unless the velocities carry
+    // the species' relative-velocity term
+    const bool bc_term = vel && ic->psi_bc;
+    if (sp == 0 || bc_term) {
       LaunchScope ls(c, KK_POINTWISE);
-      k_phitot<T><<<blocks_for(nk), kThreads, 0, s>>>((cplx<T>*)wsum, P1, p.lpt_order > 1 ? P2 : nullptr,
-                                                     p.lpt_order > 2 ? P3 : nullptr, nk, ic->dyn_d->w[pass]);
+      k_phitot<T><<<blocks_for(nk), kThreads, 0, s>>>(
+          (cplx<T>*)wsum, P1, p.lpt_order > 1 ? P2 : nullptr, p.lpt_order > 2 ? P3 : nullptr, nk, ic->dyn_d->w[pass],
+          bc_term ? (const cplx<T>*)ic->psi_bc->d : nullptr, &ic->dyn_d->wbc[sp]);
+      CK(cudaGetLastError());
     }
-    CK(cudaGetLastError());
-    void* dst = vel ? ic->dvel : ic->dpos;
+    void* dst = sp ? (vel ? ic->bvel : ic->bpos) : (vel ? ic->dvel : ic->dpos);
+    const double* qbase = sp ? ic->bqtab : ic->qtab;
     const bool three = Launch<T>::assemble3_supported(n);
     for (int ish = 0; ish < overload; ++ish) {
       if (three) {  // x pass of the three components in one launch
@@ -615,13 +781,9 @@ int enqueue_impl(mf_ic* ic) {
           op.A3[d] = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + d]->d : nullptr;
           op.dst[d] = (cplx<T>*)ic->tmp[d]->d;
         }
-        op.phase = (const cplx<T>*)ic->phase;
         op.n = n;
         op.Kz = Kz;
-        op.nstep = ish;
-        for (int st = 1; st <= ish; ++st)
-          for (int q = 0; q < 3; ++q)
-            op.s2[st - 1][q] = (int)lround(2 * (kShifts[p.lattice][st][q] - kShifts[p.lattice][st - 1][q]));
+        op.ch = lattice_chain<T>(ic->phase, p.lattice, sp == 1, ish);
         op.kfac = T(kfac);
         op.wA = &ic->dyn_d->w[pass][3];
         op.unit = T((vel ? p.vunit : p.lunit) / L);
@@ -639,15 +801,10 @@ int enqueue_impl(mf_ic* ic) {
         op.A3p = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 1) % 3]->d : nullptr;
         op.A3pp = p.lpt_order > 2 ? (const cplx<T>*)ic->f[3 + (d + 2) % 3]->d : nullptr;
         op.dst = tk;
-        op.phase = (const cplx<T>*)ic->phase;
         op.n = n;
         op.Kz = Kz;
         op.d = d;
-        // relative shifts of set_positions / set_velocities (particle_generator.hh:505-522)
-        op.nstep = ish;
-        for (int st = 1; st <= ish; ++st)
-          for (int q = 0; q < 3; ++q)
-            op.s2[st - 1][q] = (int)lround(2 * (kShifts[p.lattice][st][q] - kShifts[p.lattice][st - 1][q]));
+        op.ch = lattice_chain<T>(ic->phase, p.lattice, sp == 1, ish);
         op.kfac = T(kfac);
         op.wA = &ic->dyn_d->w[pass][3];
         op.unit = T((vel ? p.vunit : p.lunit) / L);
@@ -679,7 +836,7 @@ int enqueue_impl(mf_ic* ic) {
           CK(Launch<T>::z_c2r_plain(n / 2, PlainZOp<T>{tmpr, n, norm}, n * n, Kz, twH, twN, s));
         }
       }
-      const double* qt = ic->qtab + (size_t)ish * 3 * n;
+      const double* qt = qbase + (size_t)ish * 3 * n;
       if (three) {  // the three components' z passes with the lattice readout fused
         Lattice3Args la{};
         for (int d = 0; d < 3; ++d) la.comp[d] = ic->tmp[d]->d;
@@ -719,10 +876,39 @@ int enqueue_impl(mf_ic* ic) {
                       slice));
       }
     }
+    }  // species
+    void* dst = vel ? ic->dvel : ic->dpos;
     if (timed) CK(cudaEventRecord(ic->ev[5 + pass], s));
     if (ic->early && (fields || !MF_STREAM_HANDOFF) && !vel)  // positions final: copy them during the velocity pass
       CK(early_copy(ic->early->pos, dst, ic->pos_bytes));
     if (ic->early && fields && MF_STREAM_HANDOFF && vel) CK(early_copy(ic->early->vel, dst, ic->vel_bytes));
+  }
+  // ---- particle masses of a two-species run (ic_generator.cc:641-673) ------
+  if (p.baryons) {
+    const double pmean = 1.0 / ((double)n3 * overload);  // set_masses with munit 1 (particle_generator.hh:383)
+    for (int sp = 0; sp < 2; ++sp)
+      for (int ish = 0; ish < overload; ++ish) {
+        const T* delta = nullptr;
+        if (ic->rho_bc) {
+          cplx<T>* tk = (cplx<T>*)ic->tmp[0]->d;
+          {
+            LaunchScope ls(c, KK_POINTWISE);
+            k_shift_chain<T><<<blocks_for(nk), kThreads, 0, s>>>((const cplx<T>*)ic->rho_bc->d, tk, n,
+                                                                 lattice_chain<T>(ic->phase, p.lattice, sp == 1, ish));
+            CK(cudaGetLastError());
+          }
+          CK(fft3d_c2r<T>(c, (T*)tk, n));
+          delta = (const T*)tk;
+        }
+        LaunchScope ls(c, KK_POINTWISE);
+        if (p.pos64)
+          k_masses<T, double><<<blocks_for(n3), kThreads, 0, s>>>((double*)ic->dmass[sp], delta, n, ish, pmean, p.munit,
+                                                                  ic->dyn_d, sp);
+        else
+          k_masses<T, float><<<blocks_for(n3), kThreads, 0, s>>>((float*)ic->dmass[sp], delta, n, ish, pmean, p.munit,
+                                                                 ic->dyn_d, sp);
+        CK(cudaGetLastError());
+      }
   }
   if (timed) CK(cudaEventRecord(ic->ev[7], s));  // (the IDs are made at the start)
   if (ic->early) ic->early_all = MF_STREAM_HANDOFF;
@@ -800,7 +986,14 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   output_sizes(p, &np, &pb, &vb, &ib);
   const size_t nk2 = 3 * (size_t)(n / 2) * (n / 2) + 1;
   const size_t pltg = p->plt ? 4 * (size_t)n * n * (n / 2 + 1) * ps : 0;
-  *bytes = ngrids * grid + conv + pb + vb + ib + 2 * nk2 * sizeof(double) + pltg;
+  size_t two = 0;  // second species, masses, baryon-CDM tables and fields
+  if (p->baryons) {
+    const size_t mb = (size_t)np * (p->pos64 ? 8 : 4);
+    two = pb + vb + ib + 2 * mb + (size_t)(1 << p->lattice) * 3 * n * sizeof(double);
+    if (p->tk_dbc_table || p->tk_tbc_table)
+      two += 4 * nk2 * sizeof(double) + grid + ((p->baryon_vrel && p->tk_tbc_table) ? grid : 0);
+  }
+  *bytes = ngrids * grid + conv + pb + vb + ib + 2 * nk2 * sizeof(double) + pltg + two;
   return MF_OK;
 }
 
@@ -827,6 +1020,15 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->dpos);
   cudaFree(ic->dvel);
   cudaFree(ic->dids);
+  cudaFree(ic->bpos);
+  cudaFree(ic->bvel);
+  cudaFree(ic->bids);
+  cudaFree(ic->dmass[0]);
+  cudaFree(ic->dmass[1]);
+  cudaFree(ic->bqtab);
+  cudaFree(ic->ampbc);
+  if (ic->rho_bc) mf_grid_destroy(ic->rho_bc);
+  if (ic->psi_bc) mf_grid_destroy(ic->psi_bc);
   for (auto& e : ic->ev)
     if (e) cudaEventDestroy(e);
   cudaFree(ic->dyn_d);
@@ -866,20 +1068,20 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     // sub-lattice phase table, generated on the host in extended precision
     const long double pi = 3.141592653589793238462643383279502884L;
     const size_t ps = (p->precision == MF_PREC_F32) ? sizeof(float2) : sizeof(double2);
-    std::vector<double> re(2 * n), im(2 * n);
-    for (int m = 0; m < 2 * n; ++m) {
-      const long double a = pi * (long double)m / (long double)n;
+    std::vector<double> re(4 * n), im(4 * n);
+    for (int m = 0; m < 4 * n; ++m) {  // exp(2 pi i m / 4n)
+      const long double a = pi * (long double)m / (2.0L * (long double)n);
       re[m] = (double)cosl(a);
       im[m] = (double)sinl(a);
-      if ((2 * m) % n == 0) {  // exact on the axes
-        const int q = (2 * m) / n;
+      if (m % n == 0) {  // exact on the axes
+        const int q = m / n;
         const double cq[4] = {1, 0, -1, 0}, sq[4] = {0, 1, 0, -1};
         re[m] = cq[q];
         im[m] = sq[q];
       }
     }
-    std::vector<unsigned char> h(ps * 2 * n);
-    for (int m = 0; m < 2 * n; ++m) {
+    std::vector<unsigned char> h(ps * 4 * n);
+    for (int m = 0; m < 4 * n; ++m) {
       if (p->precision == MF_PREC_F32) reinterpret_cast<float2*>(h.data())[m] = make_float2((float)re[m], (float)im[m]);
       else reinterpret_cast<double2*>(h.data())[m] = make_double2(re[m], im[m]);
     }
@@ -974,6 +1176,51 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
   if ((e = cudaMalloc(&ic->dvel, ic->vel_bytes)) != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: velocities"));
   if (ic->id_bytes && (e = cudaMalloc(&ic->dids, ic->id_bytes)) != cudaSuccess)
     return fail(cuda_err(c, e, "mf_ic_create: ids"));
+  if (p->baryons) {
+    ic->p.tk_dbc_table = ic->p.tk_tbc_table = nullptr;  // host tables are copied, not kept
+    ic->mass_bytes = (size_t)ic->npart * (p->pos64 ? 8 : 4);
+    if ((e = cudaMalloc(&ic->bpos, ic->pos_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&ic->bvel, ic->vel_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&ic->bids, ic->id_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&ic->dmass[0], ic->mass_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&ic->dmass[1], ic->mass_bytes)) != cudaSuccess)
+      return fail(cuda_err(c, e, "mf_ic_create: baryon particles"));
+    // secondary-lattice coordinates: get_unit_r_shifted with lattice_shifts[ish]
+    // + second_lattice_shift (particle_generator.hh:531)
+    const int ov = 1 << p->lattice;
+    std::vector<double> q((size_t)ov * 3 * n);
+    for (int ish = 0; ish < ov; ++ish)
+      for (int d = 0; d < 3; ++d)
+        for (int i = 0; i < n; ++i)
+          q[((size_t)ish * 3 + d) * n + i] =
+              ((double)i + (kShifts[p->lattice][ish][d] + kSecondShift[p->lattice][d])) / (double)n * p->lunit;
+    if ((e = cudaMalloc(&ic->bqtab, q.size() * sizeof(double))) != cudaSuccess ||
+        (e = cudaMemcpy(ic->bqtab, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(cuda_err(c, e, "mf_ic_create: secondary lattice table"));
+    const bool has_d = p->tk_dbc_table != nullptr;
+    const bool has_t = p->tk_tbc_table != nullptr;
+    if (has_d || has_t) {
+      const size_t nk2 = (size_t)ic->nk2;
+      if ((e = cudaMalloc(&ic->ampbc, sizeof(double) * 4 * nk2)) != cudaSuccess)
+        return fail(cuda_err(c, e, "mf_ic_create: baryon-CDM tables"));
+      if (has_d) {
+        if ((e = cudaMemcpy(ic->ampbc + 2 * nk2, p->tk_dbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+          return fail(cuda_err(c, e, "mf_ic_create: T_delta_bc table"));
+        ic->tdbc_d = ic->ampbc + 2 * nk2;
+      }
+      if (has_t) {
+        if ((e = cudaMemcpy(ic->ampbc + 3 * nk2, p->tk_tbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+          return fail(cuda_err(c, e, "mf_ic_create: T_theta_bc table"));
+        ic->ttbc_d = ic->ampbc + 3 * nk2;
+      }
+      // rho_bc feeds the masses; psi_bc only with the relative-velocity mode
+      if ((rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->rho_bc))) return fail(rc);
+      if (p->baryon_vrel && has_t && (rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->psi_bc)))
+        return fail(rc);
+    }
+  }
   for (auto& ev : ic->ev)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) return fail(cuda_err(c, e, "mf_ic_create: events"));
   *out = ic;
@@ -1019,7 +1266,8 @@ extern "C" int mf_ic_set_noise_seed(mf_ic* ic, uint64_t seed) {
 extern "C" int mf_ic_set_cosmology(mf_ic* ic, const mf_cosmo_scalars* cosmo) {
   if (!ic || !cosmo) return MF_ERR_ARG;
   if (!(cosmo->pnorm > 0) || !(cosmo->Dplus > 0)) return set_err(ic->ctx, MF_ERR_ARG, "mf_ic_set_cosmology: bad scalars");
-  if (ic->has_tk) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_set_cosmology: the pipeline uses a tabulated T(k)");
+  if (ic->has_tk || ic->ampbc)
+    return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_set_cosmology: the pipeline uses a tabulated T(k)");
   ic->p.cosmo = *cosmo;
   fill_dyn(ic);
   return MF_OK;
@@ -1045,6 +1293,7 @@ extern "C" int mf_ic_enqueue(mf_ic* ic) {
 
 extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
+  if (ic->p.baryons) return set_err(ic->ctx, MF_ERR_ARG, "mf_ic_run: a two-species pipeline runs with mf_ic_run_species");
   if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
   ic->early = nullptr;
   ic->early_all = false;
@@ -1082,6 +1331,65 @@ extern "C" int mf_ic_particles(mf_ic* ic, mf_particles* out) {
 namespace mf {
 const mf_ic_params* ic_params(const mf_ic* ic) { return &ic->p; }
 }  // namespace mf
+
+extern "C" int mf_ic_particles_species(mf_ic* ic, int species, mf_particles* out) {
+  if (!ic || !out || species < MF_SPECIES_DM || species > (ic->p.baryons ? MF_SPECIES_BARYON : MF_SPECIES_DM))
+    return MF_ERR_ARG;
+  const bool b = species == MF_SPECIES_BARYON;
+  out->pos = b ? ic->bpos : ic->dpos;
+  out->vel = b ? ic->bvel : ic->dvel;
+  out->ids = b ? ic->bids : ic->dids;
+  out->mass = ic->dmass[b ? 1 : 0];
+  out->npart = ic->npart;
+  out->location = MF_LOC_DEVICE;
+  return MF_OK;
+}
+
+extern "C" int mf_ic_run_species(mf_ic* ic, mf_particles* out, int nspecies) {
+  if (!ic) return MF_ERR_ARG;
+  mf_ctx* c = ic->ctx;
+  if (!ic->p.baryons) return set_err(c, MF_ERR_ARG, "mf_ic_run_species: the pipeline has one species (use mf_ic_run)");
+  if (!out || nspecies != 2) return set_err(c, MF_ERR_ARG, "mf_ic_run_species: two species expected");
+  if (!ic->noise_set && !ic->noise_seeded) return set_err(c, MF_ERR_STATE, "mf_ic_run_species: white noise not set");
+  for (int sp = 0; sp < 2; ++sp)
+    if (out[sp].location == MF_LOC_HOST && (!out[sp].pos || !out[sp].vel || !out[sp].ids || !out[sp].mass))
+      return set_err(c, MF_ERR_ARG, "mf_ic_run_species: null host buffer");
+  ic->early = nullptr;  // the hand-off happens after the run
+  ic->early_all = false;
+  ic->pos_early = false;
+  int rc = mf_ic_enqueue(ic);
+  cudaError_t e = cudaSuccess;
+  for (int sp = 0; sp < 2 && rc == MF_OK; ++sp) {
+    mf_particles dev{};
+    mf_ic_particles_species(ic, sp, &dev);
+    mf_particles& o = out[sp];
+    o.npart = ic->npart;
+    if (o.location == MF_LOC_HOST) {
+      const void* src[4] = {dev.pos, dev.vel, dev.ids, dev.mass};
+      void* dst[4] = {o.pos, o.vel, o.ids, o.mass};
+      const size_t bytes[4] = {ic->pos_bytes, ic->vel_bytes, ic->id_bytes, ic->mass_bytes};
+      for (int a = 0; a < 4 && e == cudaSuccess; ++a)
+        e = cudaMemcpyAsync(dst[a], src[a], bytes[a], cudaMemcpyDeviceToHost, c->stream);
+    } else {
+      o = dev;
+    }
+  }
+  if (rc == MF_OK && e == cudaSuccess) e = cudaEventRecord(ic->ev[8], c->stream);
+  if (rc == MF_OK && e != cudaSuccess) rc = cuda_err(c, e, "mf_ic_run_species: hand-off");
+  if (rc == MF_OK) rc = check_device_error(c);
+  else cudaStreamSynchronize(c->stream);
+  return rc;
+}
+
+extern "C" int mf_ic_mass_bytes(const mf_ic_params* p, size_t* bytes) {
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (!bytes) return MF_ERR_ARG;
+  int64_t np; size_t pb, vb, ib;
+  output_sizes(p, &np, &pb, &vb, &ib);
+  *bytes = p->baryons ? (size_t)np * (p->pos64 ? 8 : 4) : 0;
+  return MF_OK;
+}
 
 extern "C" int mf_ic_context(mf_ic* ic, mf_ctx** out) {
   if (!ic || !out) return MF_ERR_ARG;

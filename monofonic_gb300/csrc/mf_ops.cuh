@@ -284,11 +284,57 @@ struct ConvXFwdOp {
   __device__ __forceinline__ void store_z(int, int j, int xx, int kz, C v) const { store(j, xx, kz, v); }
 };
 
+// Sub-lattice phase chain: the shift_field calls (grid_fft.hh:832-842) that
+// set_positions / set_velocities / set_masses (particle_generator.hh:369-639)
+// apply in sequence, each a shift dS of the field by a fraction of a cell.
+// Shifts are in quarter cells (s4 = 4 dS: the relative sub-lattice shifts are
+// multiples of 1/2, the secondary-lattice shift of RSC is 1/4), the phases
+// exp(i dS.k dx) are read from an exact table exp(+2 pi i m / 4n).
+template <typename T>
+struct ShiftChain {
+  using C = cplx<T>;
+  const C* phase;  // 4n entries exp(+2 pi i m / 4n)
+  int nstep;
+  int s4[8][3];
+  // phase of step s at (i, j, kz), k = get_k (Nyquist index positive)
+  __device__ __forceinline__ C step_phase(int s, int n, int i, int j, int kz) const {
+    const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
+    int m = (s4[s][0] * ii + s4[s][1] * jj + s4[s][2] * kz) % (4 * n);
+    if (m < 0) m += 4 * n;
+    return phase[m];
+  }
+  // Apply the chain to K values v at (i, j, kz).  The reference re-projects
+  // onto real fields (r2c of the c2r) before every shift; on the kz = 0 and
+  // kz = n/2 planes that projection pairs k with -k, H(X)(k) = (X(k) +
+  // conj X(-k)) / 2, so there vm must hold the values at (-i, -j, kz).
+  template <int K>
+  __device__ __forceinline__ void apply(int n, int i, int j, int kz, C (&v)[K], C (&vm)[K]) const {
+    if (kz == 0 || kz == (n >> 1)) {
+      const int im = (n - i) % n, jm = (n - j) % n;
+      for (int s = 0; s < nstep; ++s) {
+        const C pk = step_phase(s, n, i, j, kz), pm = step_phase(s, n, im, jm, kz);
+#pragma unroll
+        for (int d = 0; d < K; ++d) {
+          const C hk = mkc<T>(T(0.5) * (v[d].x + vm[d].x), T(0.5) * (v[d].y - vm[d].y));
+          const C hm = mkc<T>(T(0.5) * (vm[d].x + v[d].x), T(0.5) * (vm[d].y - v[d].y));
+          v[d] = cmul(hk, pk);
+          vm[d] = cmul(hm, pm);
+        }
+      }
+      return;
+    }
+    for (int s = 0; s < nstep; ++s) {
+      const C ph = step_phase(s, n, i, j, kz);
+#pragma unroll
+      for (int d = 0; d < K; ++d) v[d] = cmul(v[d], ph);
+    }
+  }
+};
+
 // x pass of the c2r of one displacement / velocity component, with the
 // k-space assembly of ic_generator.cc:829-858 / :884-931 fused into the load:
 //   i g_d phitot + w_A (i g_d' A3[d''] - i g_d'' A3[d']), times unit/L, zero DC,
-// times the sub-lattice phase exp(i s.k dx) of shift_field (grid_fft.hh:832-842)
-// read from an exact table exp(+2 pi i m / 2n), m = sum_d 2 s_d k_d mod 2n.
+// times the sub-lattice phase chain (ShiftChain).
 // slab = j, e = i, col = kz; in place on the destination grid.
 template <typename T>
 struct AssembleXInvOp {
@@ -297,12 +343,8 @@ struct AssembleXInvOp {
   const C* A3p;     // A3[d'] (nullptr below 3LPT)
   const C* A3pp;    // A3[d'']
   C* dst;
-  const C* phase;   // 2n entries exp(+2 pi i m / 2n)
   int n, Kz, d;
-  // sub-lattice: nstep relative shifts (shift_field calls of
-  // particle_generator.hh:505-522), each 2*(s_ish - s_{ish-1}) in {-1,0,1}
-  int nstep;
-  int s2[7][3];
+  ShiftChain<T> ch;
   T kfac, unit;
   const double* wA;  // device scalar: weight of the A3 term (growth factor of this pass)
   int plt;          // PLT corrected gradient (lattice_gradient, particle_plt.hh:551-573)
@@ -351,33 +393,13 @@ struct AssembleXInvOp {
     }
     return mkc<T>(rr * unit, ri * unit);
   }
-  // phase of relative shift step s at (i, j, kz): exp(i dS.k dx), k = get_k
-  // (Nyquist index positive), dS = s2/2
-  __device__ __forceinline__ C step_phase(int s, int i, int j, int kz) const {
-    const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
-    int m = (s2[s][0] * ii + s2[s][1] * jj + s2[s][2] * kz) % (2 * n);
-    if (m < 0) m += 2 * n;
-    return phase[m];
-  }
   __device__ __forceinline__ C load(int j, int i, int kz) const {
-    C v = assemble(i, j, kz);
-    if (nstep == 0) return v;
-    if (kz == 0 || kz == (n >> 1)) {
-      // the reference re-projects onto real fields (r2c of the c2r) before
-      // every shift; on the kz = 0 and kz = n/2 planes that projection pairs
-      // k with -k: H(X)(k) = (X(k) + conj X(-k)) / 2
-      const int im = (n - i) % n, jm = (n - j) % n;
-      C vm = assemble(im, jm, kz);
-      for (int s = 0; s < nstep; ++s) {
-        const C hk = mkc<T>(T(0.5) * (v.x + vm.x), T(0.5) * (v.y - vm.y));
-        const C hm = mkc<T>(T(0.5) * (vm.x + v.x), T(0.5) * (vm.y - v.y));
-        v = cmul(hk, step_phase(s, i, j, kz));
-        vm = cmul(hm, step_phase(s, im, jm, kz));
-      }
-      return v;
-    }
-    for (int s = 0; s < nstep; ++s) v = cmul(v, step_phase(s, i, j, kz));
-    return v;
+    C v[1] = {assemble(i, j, kz)};
+    if (ch.nstep == 0) return v[0];
+    C vm[1] = {mkc<T>(T(0), T(0))};
+    if (kz == 0 || kz == (n >> 1)) vm[0] = assemble((n - i) % n, (n - j) % n, kz);
+    ch.apply<1>(n, i, j, kz, v, vm);
+    return v[0];
   }
   __device__ __forceinline__ void store(int j, int i, int kz, C v) const { dst[((long long)i * n + j) * Kz + kz] = v; }
 };
@@ -440,10 +462,8 @@ struct Assemble3XInvOp {
   const C* phitot;
   const C* A3[3];  // nullptr below 3LPT
   C* dst[3];
-  const C* phase;
   int n, Kz;
-  int nstep;
-  int s2[7][3];
+  ShiftChain<T> ch;
   T kfac, unit;
   const double* wA;
   int plt, vel;
@@ -490,37 +510,13 @@ struct Assemble3XInvOp {
       o[d] = mkc<T>(rr * unit, ri * unit);
     }
   }
-  __device__ __forceinline__ C step_phase(int s, int i, int j, int kz) const {
-    const int ii = i - ((i > (n >> 1)) ? n : 0), jj = j - ((j > (n >> 1)) ? n : 0);
-    int m = (s2[s][0] * ii + s2[s][1] * jj + s2[s][2] * kz) % (2 * n);
-    if (m < 0) m += 2 * n;
-    return phase[m];
-  }
   // slab = j, e = i, col = kz
   __device__ __forceinline__ void load3(int j, int i, int kz, C (&v)[3]) const {
     assemble(i, j, kz, v);
-    if (nstep == 0) return;
-    if (kz == 0 || kz == (n >> 1)) {
-      const int im = (n - i) % n, jm = (n - j) % n;
-      C vm[3];
-      assemble(im, jm, kz, vm);
-      for (int s = 0; s < nstep; ++s) {
-        const C pk = step_phase(s, i, j, kz), pm = step_phase(s, im, jm, kz);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const C hk = mkc<T>(T(0.5) * (v[d].x + vm[d].x), T(0.5) * (v[d].y - vm[d].y));
-          const C hm = mkc<T>(T(0.5) * (vm[d].x + v[d].x), T(0.5) * (vm[d].y - v[d].y));
-          v[d] = cmul(hk, pk);
-          vm[d] = cmul(hm, pm);
-        }
-      }
-      return;
-    }
-    for (int s = 0; s < nstep; ++s) {
-      const C ph = step_phase(s, i, j, kz);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = cmul(v[d], ph);
-    }
+    if (ch.nstep == 0) return;
+    C vm[3];
+    if (kz == 0 || kz == (n >> 1)) assemble((n - i) % n, (n - j) % n, kz, vm);
+    ch.apply<3>(n, i, j, kz, v, vm);
   }
   __device__ __forceinline__ void store(int d, int j, int i, int kz, C v) const {
     dst[d][((long long)i * n + j) * Kz + kz] = v;

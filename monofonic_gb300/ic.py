@@ -85,8 +85,12 @@ class ICConfig:
     id64: bool = True
     plt_ngrid: int = 0
     per_term_conv: bool = False
+    baryons: bool = False       # setup/DoBaryons: dark matter + baryon particles with masses
+    baryon_vrel: bool = False   # setup/DoBaryonVrel
+    munit: float = 1.0          # output_plugin::mass_unit
+    Dplus_target: float = 0.0   # D+ at ztarget (0: 1)
 
-    def to_c(self, scalars, tk_table=None):
+    def to_c(self, scalars, tk_table=None, tk_dbc=None, tk_tbc=None):
         p = L.mf_ic_params()
         p.ngrid = self.ngrid
         p.boxlen = self.boxlen
@@ -107,16 +111,25 @@ class ICConfig:
         p.id64 = int(self.id64)
         p.plt_ngrid = int(self.plt_ngrid)
         p.per_term_conv = int(self.per_term_conv)
+        p.baryons = int(self.baryons)
+        p.baryon_vrel = int(self.baryon_vrel)
+        p.munit = float(self.munit)
+        p.tk_dbc_table = tk_dbc.ctypes.data if tk_dbc is not None else None
+        p.tk_tbc_table = tk_tbc.ctypes.data if tk_tbc is not None else None
+        p.Dplus_target = float(self.Dplus_target)
         return p
 
 
 class ICGenerator:
     """Device-resident LPT pipeline for one parameter set."""
 
-    def __init__(self, ctx: Context, cfg: ICConfig, scalars, tk_table=None):
+    def __init__(self, ctx: Context, cfg: ICConfig, scalars, tk_table=None, tk_dbc=None, tk_tbc=None):
+        """tk_table, tk_dbc, tk_tbc: optional host tables of T_delta_matter,
+        T_delta_bc and T_theta_bc at k = sqrt(k2)*2pi/L, k2 = 0..3(n/2)^2"""
         self.ctx, self.cfg = ctx, cfg
-        self._tk = None if tk_table is None else np.ascontiguousarray(tk_table, dtype=np.float64)
-        self.params = cfg.to_c(scalars, self._tk)
+        as64 = lambda t: None if t is None else np.ascontiguousarray(t, dtype=np.float64)
+        self._tk, self._tdbc, self._ttbc = as64(tk_table), as64(tk_dbc), as64(tk_tbc)
+        self.params = cfg.to_c(scalars, self._tk, self._tdbc, self._ttbc)
         p = C.c_void_p()
         _check(ctx.ptr, lib().mf_ic_create(ctx.ptr, C.byref(self.params), C.byref(p)))
         self.ptr = p
@@ -175,6 +188,28 @@ class ICGenerator:
         out.location = L.MF_LOC_DEVICE
         _check(self.ctx.ptr, lib().mf_ic_run(self.ptr, C.byref(out)))
         return out.pos, out.vel, out.ids
+
+    def run_species(self, to_host: bool = True):
+        """two-species run (cfg.baryons): {"dm": (pos, vel, ids, mass),
+        "baryon": (...)} as numpy arrays, or device pointers"""
+        outs = (L.mf_particles * 2)()
+        keep = []
+        if to_host:
+            cfg = self.cfg
+            rt = np.float64 if cfg.pos64 else np.float32
+            for sp in range(2):
+                arrs = (np.empty((self.npart, 3), dtype=rt), np.empty((self.npart, 3), dtype=rt),
+                        np.empty(self.npart, dtype=np.uint64 if cfg.id64 else np.uint32), np.empty(self.npart, dtype=rt))
+                keep.append(arrs)
+                outs[sp].pos, outs[sp].vel, outs[sp].ids, outs[sp].mass = (a.ctypes.data for a in arrs)
+                outs[sp].location = L.MF_LOC_HOST
+        else:
+            for sp in range(2):
+                outs[sp].location = L.MF_LOC_DEVICE
+        _check(self.ctx.ptr, lib().mf_ic_run_species(self.ptr, outs, 2))
+        if to_host:
+            return {"dm": keep[0], "baryon": keep[1]}
+        return {k: (outs[i].pos, outs[i].vel, outs[i].ids, outs[i].mass) for i, k in enumerate(("dm", "baryon"))}
 
     def stage_times(self):
         ms = (C.c_double * 8)()

@@ -516,6 +516,7 @@ class LPTFields:
     phi2: np.ndarray | None
     phi3: np.ndarray | None
     A3: list | None
+    wn: np.ndarray | None = None  # normalised k-space white noise (ic_generator.cc:341-346)
 
 
 def amplitude(kmod, cs, eh):
@@ -595,7 +596,7 @@ def lpt_potentials(noise_r, L, order, cs, eh=None, convolver="orszag", fixing=Fa
     if order > 2:
         phi3 = phi3 * g3
         A3 = [a * g3c for a in A3]
-    return LPTFields(phi, phi2, phi3, A3)
+    return LPTFields(phi, phi2, phi3, A3, wn)
 
 
 # ----------------------------------------------------------------------------
@@ -653,36 +654,44 @@ def shift_field(fr, s, L):
     return c2r(F, n)
 
 
-def lattice_positions_component(field_r, d, lattice, unit, L):
-    """set_positions, Bravais branch (particle_generator.hh:499-544), one
-    component d: returns the overload*n^3 values pos[ip] in particle order
-    ishift*n^3 + cell."""
-    n = field_r.shape[0]
+SECOND_LATTICE_SHIFT = {  # particle_generator.hh:56-63
+    0: (0.5, 0.5, 0.5), 1: (0.5, 0.5, 0.0), 2: (0.5, 0.5, 0.5), 3: (0.25, 0.25, 0.25)}
+
+
+def _sublattice_fields(field_r, lattice, L, secondary=False):
+    """the field read out on each sub-lattice: the secondary lattice's global
+    shift first, then the relative shifts (particle_generator.hh:389-401,
+    :510-522, :607-618), each a shift_field round trip"""
     shifts = LATTICE_SHIFTS[lattice]
-    out = []
     fr = field_r
-    idx = np.arange(n, dtype=np.float64)
     for ish, s in enumerate(shifts):
+        if ish == 0 and secondary:
+            fr = shift_field(fr, SECOND_LATTICE_SHIFT[lattice], L)
         if ish > 0:
             prev = shifts[ish - 1]
             fr = shift_field(fr, tuple(s[a] - prev[a] for a in range(3)), L)
-        q = (idx + s[d]) / float(n)
+        yield ish, s, fr
+
+
+def lattice_positions_component(field_r, d, lattice, unit, L, secondary=False):
+    """set_positions, Bravais branch (particle_generator.hh:499-544), one
+    component d: returns the overload*n^3 values pos[ip] in particle order
+    ishift*n^3 + cell; the secondary lattice adds second_lattice_shift to q
+    (particle_generator.hh:531)."""
+    n = field_r.shape[0]
+    out = []
+    idx = np.arange(n, dtype=np.float64)
+    for ish, s, fr in _sublattice_fields(field_r, lattice, L, secondary):
+        sd = s[d] + (SECOND_LATTICE_SHIFT[lattice][d] if secondary else 0.0)
+        q = (idx + sd) / float(n)
         qg = [q[:, None, None], q[None, :, None], q[None, None, :]][d]
         out.append((qg * unit + fr).reshape(-1))
     return np.concatenate(out)
 
 
-def lattice_velocities_component(field_r, lattice, L):
+def lattice_velocities_component(field_r, lattice, L, secondary=False):
     """set_velocities, Bravais branch (particle_generator.hh:597-639)."""
-    shifts = LATTICE_SHIFTS[lattice]
-    out = []
-    fr = field_r
-    for ish, s in enumerate(shifts):
-        if ish > 0:
-            prev = shifts[ish - 1]
-            fr = shift_field(fr, tuple(s[a] - prev[a] for a in range(3)), L)
-        out.append(fr.reshape(-1))
-    return np.concatenate(out)
+    return np.concatenate([fr.reshape(-1) for _, _, fr in _sublattice_fields(field_r, lattice, L, secondary)])
 
 
 def particle_ids(n, lattice, id_offset=0):
@@ -712,6 +721,67 @@ def particles(f: LPTFields, L, order, vfac, lattice=0, lunit=1.0, vunit=1.0):
         fr = c2r(displacement_k(f, L, d, order, unit=vunit, vel=True, vfac=vfac), n)
         vel[:, d] = lattice_velocities_component(fr, lattice, L)
     return pos, vel, particle_ids(n, lattice)
+
+
+# ----------------------------------------------------------------------------
+# two species: dark matter and baryons (ic_generator.cc:153-166, :608-948)
+# ----------------------------------------------------------------------------
+def bc_amplitudes(kmod, cs, Tdbc, Ttbc, vrel, Dplus_target=1.0):
+    """get_amplitude_delta_bc / get_amplitude_theta_bc
+    (cosmology_calculator.hh:416-431); Tdbc, Ttbc callables of k or None (0,
+    as the Eisenstein-Hu plugin returns)"""
+    zero = lambda k: np.zeros_like(k)
+    Td = (Tdbc or zero)(kmod)
+    Tt = (Ttbc or zero)(kmod)
+    sDr = math.sqrt(Dplus_target / cs.Dplus)
+    pk = np.power(kmod, 0.5 * cs.n_s)
+    dbc = Td + (2 * Tt * (sDr - 1.0) if vrel else 0.0)
+    a_d = pk * dbc * (math.sqrt(cs.pnorm) * Dplus_target)
+    a_t = pk * (Tt * sDr) * (math.sqrt(cs.pnorm) * Dplus_target) if vrel else np.zeros_like(kmod)
+    return a_d, a_t
+
+
+def two_species_particles(f: LPTFields, L, order, cs, Omega_m, Omega_b, lattice=0, lunit=1.0, vunit=1.0, munit=1.0,
+                          Tdbc=None, Ttbc=None, vrel=False, Dplus_target=1.0):
+    """DoBaryons with a particle output plugin: per species (dm, baryon) the
+    positions, velocities, ids and masses.  Baryons sit on the secondary
+    lattice and take IDoffset 1 (ic_generator.cc:626-637); the masses are
+    pmeanmass (1 + C_s delta_bc) Omega_s munit (:641-673, set_masses
+    particle_generator.hh:369-422); with DoBaryonVrel the velocities carry
+    -vfac C_s amp_tbc wn grad / k^2 (:907-910)."""
+    n = f.phi.shape[0]
+    overload = 1 << max(0, lattice)
+    kx, ky, kz = kgrids(n, L)
+    kmod = np.sqrt(kx * kx + ky * ky + kz * kz)
+    a_d, a_t = bc_amplitudes(kmod, cs, Tdbc, Ttbc, vrel, Dplus_target)
+    rho_k = f.wn * a_d
+    rho_k[0, 0, 0] = 0
+    delta = c2r(rho_k, n)
+    fb = Omega_b / Omega_m
+    g = ggrids(n, L)
+    out = {}
+    for sp, name in enumerate(("dm", "baryon")):
+        C = (1.0 - fb) if name == "baryon" else -fb
+        Om_s = Omega_b if name == "baryon" else Omega_m - Omega_b
+        sec = name == "baryon"
+        pos = np.empty((overload * n ** 3, 3))
+        vel = np.empty((overload * n ** 3, 3))
+        for d in range(3):
+            fr = c2r(displacement_k(f, L, d, order, unit=lunit), n)
+            pos[:, d] = lattice_positions_component(fr, d, lattice, lunit, L, secondary=sec)
+        for d in range(3):
+            t = displacement_k(f, L, d, order, unit=vunit, vel=True, vfac=cs.vfac)
+            if vrel:
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    bc = -cs.vfac * C * a_t * f.wn * (1j * g[d]) / (kmod * kmod)
+                bc[0, 0, 0] = 0
+                t = t + bc * (vunit / L)
+            vel[:, d] = lattice_velocities_component(c2r(t, n), lattice, L, secondary=sec)
+        rho = (1.0 + C * delta) * Om_s * munit
+        pmean = 1.0 / (n ** 3 * overload)
+        mass = np.concatenate([pmean * fr.reshape(-1) for _, _, fr in _sublattice_fields(rho, lattice, L, sec)])
+        out[name] = (pos, vel, particle_ids(n, lattice, id_offset=sp), mass)
+    return out
 
 
 # ----------------------------------------------------------------------------
