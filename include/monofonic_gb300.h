@@ -137,6 +137,10 @@ int mf_grid_shift(mf_grid* g, const double s[3], int transform_back);
  * *nbins receives int(kmax/kmin) */
 int mf_grid_power_spectrum(mf_grid* g, double* bin_k, double* bin_P, double* bin_eP,
                            int64_t* bin_count, int nbins_cap, int* nbins);
+/* Grid_FFT<ccomplex_t> transforms (src/grid_fft.cc:56-63, FFTW_FORWARD /
+ * FFTW_BACKWARD, unitary): in place on an n^3 complex FP64 device array
+ * [i][j][k] on the context's stream (asynchronous) */
+int mf_cgrid_fft(mf_ctx* ctx, void* data, int n, int inverse);
 
 /* ---- convolvers (include/convolution.hh) ------------------------------- */
 typedef struct {

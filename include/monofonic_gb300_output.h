@@ -66,9 +66,11 @@ int mf_grafic2_write_grid(mf_grafic2* w, mf_grid* g, int species, int component)
  * (prec) at a device or page-locked/pageable host address (location) */
 int mf_grafic2_write_field(mf_grafic2* w, const void* field, int prec, int location, int species,
                            int component);
-/* ic_generator.cc:794-891 with a field_lagrangian plugin: run the pipeline
- * (created with out_kind MF_OUT_FIELDS and the plugin's position/velocity
- * units) and write dx, dy, dz, vx, vy, vz of the dark matter */
+/* ic_generator.cc:608-948 with this plugin: run the pipeline (created with
+ * out_kind MF_OUT_FIELDS and the plugin's position/velocity units) and write
+ * dx, dy, dz, vx, vy, vz of the dark matter (field_lagrangian); with baryons
+ * (munit = the plugin's 1/Omega_m) also the dark matter's mass field and the
+ * baryons' density and vx, vy, vz from the semiclassical Eulerian branch */
 int mf_ic_write_grafic2(mf_ic* ic, mf_grafic2* w);
 /* the last write call: bytes written to files, milliseconds of the device
  * plane-transpose launches (CUDA events on the context's stream) and of the

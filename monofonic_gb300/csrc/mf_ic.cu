@@ -13,6 +13,7 @@
 #include "mf_cosmo.h"
 #include "mf_eh.cuh"
 #include "mf_plt.h"
+#include "mf_ppt.h"
 #include "mf_runtime.h"
 
 // host hand-off during a run (a build-time knob): 0 copies the positions
@@ -51,7 +52,7 @@ struct ICDyn {
 // amplitudes of the baryon-CDM modes per integer k^2: get_amplitude_delta_bc
 // and get_amplitude_theta_bc (cosmology_calculator.hh:416-431) from the host
 // tables of T_delta_bc and T_theta_bc (zero where a table is absent)
-__global__ void k_amp_bc(double* ampd, double* ampt, int nk2, double kfac, const ICDyn* __restrict__ dyn,
+__global__ void k_amp_bc(double* ampd, double* ampt, double* ampd0, int nk2, double kfac, const ICDyn* __restrict__ dyn,
                          const double* tdbc, const double* ttbc) {
   const double half_ns = dyn->half_ns, sqrtpnorm = dyn->sqrtpnorm, Dt = dyn->bc_Dt, sDr = dyn->bc_sqrtDr;
   const int vrel = dyn->vrel;
@@ -61,6 +62,7 @@ __global__ void k_amp_bc(double* ampd, double* ampt, int nk2, double kfac, const
     const double dbc = td + (vrel ? 2 * tt * (sDr - 1.0) : 0.0);
     ampd[k2] = pow(k, half_ns) * dbc * (sqrtpnorm * Dt);
     ampt[k2] = vrel ? pow(k, half_ns) * (tt * sDr) * (sqrtpnorm * Dt) : 0.0;
+    ampd0[k2] = pow(k, half_ns) * td * (sqrtpnorm * Dt);  // without the relative-velocity mode
   }
 }
 
@@ -68,8 +70,8 @@ __global__ void k_amp_bc(double* ampd, double* ampt, int nk2, double kfac, const
 // (ic_generator.cc:655-660) and the relative-velocity potential
 // psi_bc = amp_tbc wn / k^2 (ic_generator.cc:907-910), both with zero DC
 template <typename T>
-__global__ void k_bc_fields(const cplx<T>* wn, cplx<T>* rho, cplx<T>* psi, int n, double kfac, const double* ampd,
-                            const double* ampt) {
+__global__ void k_bc_fields(const cplx<T>* wn, cplx<T>* rho, cplx<T>* psi, cplx<T>* rho0, int n, double kfac,
+                            const double* ampd, const double* ampt, const double* ampd0) {
   const int Kz = n / 2 + 1;
   const size_t tot = (size_t)n * n * Kz;
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
@@ -82,6 +84,10 @@ __global__ void k_bc_fields(const cplx<T>* wn, cplx<T>* rho, cplx<T>* psi, int n
     if (rho) {
       const T a = T(ampd[k2]);
       rho[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(w.x * a, w.y * a);
+    }
+    if (rho0) {  // the Eulerian branch's delta_bc (ic_generator.cc:685-688)
+      const T a = T(ampd0[k2]);
+      rho0[idx] = (idx == 0) ? mkc<T>(T(0), T(0)) : mkc<T>(w.x * a, w.y * a);
     }
     if (psi) {
       const T kx = T(ii) * T(kfac), ky = T(jj) * T(kfac), kk = T(kz) * T(kfac);
@@ -104,7 +110,7 @@ __global__ void k_shift_chain(const cplx<T>* src, cplx<T>* dst, int n, ShiftChai
     cplx<T> v[1] = {src[idx]};
     cplx<T> vm[1] = {mkc<T>(T(0), T(0))};
     if (kz == 0 || kz == n / 2) vm[0] = src[((size_t)((n - i) % n) * n + (n - j) % n) * Kz + kz];
-    ch.apply<1>(n, i, j, kz, v, vm);
+    ch.template apply<1>(n, i, j, kz, v, vm);
     dst[idx] = v[0];
   }
 }
@@ -307,6 +313,8 @@ struct mf_ic {
   const double* ttbc_d = nullptr;
   mf_grid* rho_bc = nullptr;  // k-space wn amp_dbc
   mf_grid* psi_bc = nullptr;  // k-space amp_tbc wn / k^2
+  mf_grid* rho_e = nullptr;   // k-space wn amp_dbc without the relative-velocity mode (Eulerian branch)
+  void* ppt = nullptr;        // Eulerian-branch scratch: two FP64 real grids, 3 n^3 complex, one scalar
   int64_t npart = 0;
   cudaEvent_t ev[9] = {};
   bool noise_set = false;   // an uploaded white-noise field is waiting in wn
@@ -348,8 +356,6 @@ int check_params(const mf_ic_params* p) {
   if (!(p->boxlen > 0)) return MF_ERR_ARG;
   if (p->plt && p->plt_ngrid != 0 && !grid_size_supported(p->plt_ngrid)) return MF_ERR_SHAPE;
   if (p->baryons) {
-    // two-species field output goes through the semiclassical Eulerian branch, not built
-    if (p->out_kind != MF_OUT_PARTICLES) return MF_ERR_ARG;
     if (!(p->munit > 0) || !(p->cosmo.Omega_b > 0) || !(p->cosmo.Omega_m > p->cosmo.Omega_b)) return MF_ERR_ARG;
     if (p->Dplus_target < 0) return MF_ERR_ARG;
   }
@@ -662,11 +668,13 @@ int enqueue_impl(mf_ic* ic) {
     LaunchScope ls(c, KK_POINTWISE);
     double* ampd = ic->ampbc;
     double* ampt = ic->ampbc + ic->nk2;
-    k_amp_bc<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ampd, ampt, ic->nk2, kfac, ic->dyn_d, ic->tdbc_d, ic->ttbc_d);
+    double* ampd0 = ic->ampbc + 2 * ic->nk2;
+    k_amp_bc<<<(ic->nk2 + 255) / 256, 256, 0, s>>>(ampd, ampt, ampd0, ic->nk2, kfac, ic->dyn_d, ic->tdbc_d,
+                                                   ic->ttbc_d);
     CK(cudaGetLastError());
-    k_bc_fields<T><<<blocks_for(nk), kThreads, 0, s>>>((const cplx<T>*)ic->wn->d, (cplx<T>*)ic->rho_bc->d,
-                                                        ic->psi_bc ? (cplx<T>*)ic->psi_bc->d : nullptr, n, kfac, ampd,
-                                                        ampt);
+    k_bc_fields<T><<<blocks_for(nk), kThreads, 0, s>>>(
+        (const cplx<T>*)ic->wn->d, (cplx<T>*)ic->rho_bc->d, ic->psi_bc ? (cplx<T>*)ic->psi_bc->d : nullptr,
+        ic->rho_e ? (cplx<T>*)ic->rho_e->d : nullptr, n, kfac, ampd, ampt, ampd0);
     CK(cudaGetLastError());
   }
   if (timed) CK(cudaEventRecord(ic->ev[1], s));
@@ -756,7 +764,9 @@ int enqueue_impl(mf_ic* ic) {
   const cplx<T>* twH = c->tw.get<T>(n / 2, s);
   if (!twN || !twH) return set_err(c, MF_ERR_OOM, "twiddles");
   const size_t n3 = (size_t)n * n * n;
-  const int nsp = p.baryons ? 2 : 1;  // species: dark matter, then baryons on the secondary lattice
+  // species of the Lagrangian assembly: dark matter, then the baryons on the
+  // secondary lattice; with field output the baryons take the Eulerian branch
+  const int nsp = (p.baryons && !fields) ? 2 : 1;
   for (int pass = 0; pass < 2; ++pass) {  // 0: positions, 1: velocities
     const bool vel = pass == 1;
     for (int sp = 0; sp < nsp; ++sp) {
@@ -883,10 +893,12 @@ int enqueue_impl(mf_ic* ic) {
       CK(early_copy(ic->early->pos, dst, ic->pos_bytes));
     if (ic->early && fields && MF_STREAM_HANDOFF && vel) CK(early_copy(ic->early->vel, dst, ic->vel_bytes));
   }
-  // ---- particle masses of a two-species run (ic_generator.cc:641-673) ------
+  // ---- particle masses of a two-species run (ic_generator.cc:641-673): per
+  // particle, or the dark matter's mass field for field output ---------------
   if (p.baryons) {
-    const double pmean = 1.0 / ((double)n3 * overload);  // set_masses with munit 1 (particle_generator.hh:383)
-    for (int sp = 0; sp < 2; ++sp)
+    // set_masses with munit 1 (particle_generator.hh:383); a field is written as is
+    const double pmean = fields ? 1.0 : 1.0 / ((double)n3 * overload);
+    for (int sp = 0; sp < (fields ? 1 : 2); ++sp)
       for (int ish = 0; ish < overload; ++ish) {
         const T* delta = nullptr;
         if (ic->rho_bc) {
@@ -901,7 +913,7 @@ int enqueue_impl(mf_ic* ic) {
           delta = (const T*)tk;
         }
         LaunchScope ls(c, KK_POINTWISE);
-        if (p.pos64)
+        if (p.pos64 || fields)
           k_masses<T, double><<<blocks_for(n3), kThreads, 0, s>>>((double*)ic->dmass[sp], delta, n, ish, pmean, p.munit,
                                                                   ic->dyn_d, sp);
         else
@@ -909,6 +921,32 @@ int enqueue_impl(mf_ic* ic) {
                                                                  ic->dyn_d, sp);
         CK(cudaGetLastError());
       }
+  }
+  // ---- baryons of a two-species field output: the semiclassical Eulerian
+  // branch (ic_generator.cc:679-791) --------------------------------------------
+  if (p.baryons && fields) {
+    PPTArgs a{};
+    a.n = n;
+    a.L = L;
+    a.f0 = ic->f[0]->d;
+    a.f1 = p.lpt_order > 1 ? ic->f[1]->d : nullptr;
+    a.g1 = ic->dyn_h->w[0][0];
+    a.g2 = ic->dyn_h->w[0][1];
+    mf_grid* de = ic->rho_e ? ic->rho_e : ic->rho_bc;
+    a.delta_k = de ? de->d : nullptr;
+    a.delta_r = ic->tmp[1]->d;
+    a.C = ic->dyn_h->Cs[1];
+    a.D = p.cosmo.Dplus;
+    a.vunit = p.cosmo.Dplus * p.cosmo.vfac / L * p.vunit;
+    char* b = (char*)ic->ppt;
+    a.phi_r = (double*)b;
+    a.phi2_r = a.phi_r + grid_reals(n);
+    a.psi = (double2*)(a.phi2_r + grid_reals(n));
+    a.grad = a.psi + n3;
+    a.maxd = (double*)(a.grad + 2 * n3);
+    a.rho_out = (double*)ic->bpos;
+    a.vel_out = (double*)ic->bvel;
+    CK((p.precision == MF_PREC_F64) ? ppt_eulerian<double>(c, a) : ppt_eulerian<float>(c, a));
   }
   if (timed) CK(cudaEventRecord(ic->ev[7], s));  // (the IDs are made at the start)
   if (ic->early) ic->early_all = MF_STREAM_HANDOFF;
@@ -988,10 +1026,13 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
   const size_t pltg = p->plt ? 4 * (size_t)n * n * (n / 2 + 1) * ps : 0;
   size_t two = 0;  // second species, masses, baryon-CDM tables and fields
   if (p->baryons) {
-    const size_t mb = (size_t)np * (p->pos64 ? 8 : 4);
-    two = pb + vb + ib + 2 * mb + (size_t)(1 << p->lattice) * 3 * n * sizeof(double);
+    const bool fl = p->out_kind == MF_OUT_FIELDS;
+    const size_t mb = (size_t)np * ((p->pos64 || fl) ? 8 : 4);
+    two = pb + vb + ib + (fl ? 1 : 2) * mb + (size_t)(1 << p->lattice) * 3 * n * sizeof(double);
+    if (fl) two += 2 * grid_reals(n) * sizeof(double) + 3 * (size_t)n * n * n * 16 + 16;
     if (p->tk_dbc_table || p->tk_tbc_table)
-      two += 4 * nk2 * sizeof(double) + grid + ((p->baryon_vrel && p->tk_tbc_table) ? grid : 0);
+      two += 5 * nk2 * sizeof(double) + grid + ((p->baryon_vrel && p->tk_tbc_table) ? grid : 0) +
+             ((fl && p->baryon_vrel) ? grid : 0);
   }
   *bytes = ngrids * grid + conv + pb + vb + ib + 2 * nk2 * sizeof(double) + pltg + two;
   return MF_OK;
@@ -1029,6 +1070,8 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->ampbc);
   if (ic->rho_bc) mf_grid_destroy(ic->rho_bc);
   if (ic->psi_bc) mf_grid_destroy(ic->psi_bc);
+  if (ic->rho_e) mf_grid_destroy(ic->rho_e);
+  cudaFree(ic->ppt);
   for (auto& e : ic->ev)
     if (e) cudaEventDestroy(e);
   cudaFree(ic->dyn_d);
@@ -1178,13 +1221,22 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     return fail(cuda_err(c, e, "mf_ic_create: ids"));
   if (p->baryons) {
     ic->p.tk_dbc_table = ic->p.tk_tbc_table = nullptr;  // host tables are copied, not kept
-    ic->mass_bytes = (size_t)ic->npart * (p->pos64 ? 8 : 4);
+    const bool fields = p->out_kind == MF_OUT_FIELDS;
+    // particles: per-particle masses of both species; fields: the dark
+    // matter's mass field (n^3 doubles) and the baryons' Eulerian density
+    // (first n^3 doubles of the position buffer) and velocities
+    ic->mass_bytes = fields ? (size_t)ic->npart * 8 : (size_t)ic->npart * (p->pos64 ? 8 : 4);
     if ((e = cudaMalloc(&ic->bpos, ic->pos_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&ic->bvel, ic->vel_bytes)) != cudaSuccess ||
-        (e = cudaMalloc(&ic->bids, ic->id_bytes)) != cudaSuccess ||
+        (ic->id_bytes && (e = cudaMalloc(&ic->bids, ic->id_bytes)) != cudaSuccess) ||
         (e = cudaMalloc(&ic->dmass[0], ic->mass_bytes)) != cudaSuccess ||
-        (e = cudaMalloc(&ic->dmass[1], ic->mass_bytes)) != cudaSuccess)
+        (!fields && (e = cudaMalloc(&ic->dmass[1], ic->mass_bytes)) != cudaSuccess))
       return fail(cuda_err(c, e, "mf_ic_create: baryon particles"));
+    if (fields) {
+      const size_t n3 = (size_t)n * n * n;
+      if ((e = cudaMalloc(&ic->ppt, 2 * grid_reals(n) * sizeof(double) + 3 * n3 * sizeof(double2) + 16)) != cudaSuccess)
+        return fail(cuda_err(c, e, "mf_ic_create: Eulerian-branch buffers"));
+    }
     // secondary-lattice coordinates: get_unit_r_shifted with lattice_shifts[ish]
     // + second_lattice_shift (particle_generator.hh:531)
     const int ov = 1 << p->lattice;
@@ -1201,23 +1253,27 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     const bool has_t = p->tk_tbc_table != nullptr;
     if (has_d || has_t) {
       const size_t nk2 = (size_t)ic->nk2;
-      if ((e = cudaMalloc(&ic->ampbc, sizeof(double) * 4 * nk2)) != cudaSuccess)
+      // [amp_dbc, amp_tbc, amp_dbc without vbc, T_delta_bc, T_theta_bc]
+      if ((e = cudaMalloc(&ic->ampbc, sizeof(double) * 5 * nk2)) != cudaSuccess)
         return fail(cuda_err(c, e, "mf_ic_create: baryon-CDM tables"));
       if (has_d) {
-        if ((e = cudaMemcpy(ic->ampbc + 2 * nk2, p->tk_dbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
+        if ((e = cudaMemcpy(ic->ampbc + 3 * nk2, p->tk_dbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
             cudaSuccess)
           return fail(cuda_err(c, e, "mf_ic_create: T_delta_bc table"));
-        ic->tdbc_d = ic->ampbc + 2 * nk2;
+        ic->tdbc_d = ic->ampbc + 3 * nk2;
       }
       if (has_t) {
-        if ((e = cudaMemcpy(ic->ampbc + 3 * nk2, p->tk_tbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
+        if ((e = cudaMemcpy(ic->ampbc + 4 * nk2, p->tk_tbc_table, sizeof(double) * nk2, cudaMemcpyHostToDevice)) !=
             cudaSuccess)
           return fail(cuda_err(c, e, "mf_ic_create: T_theta_bc table"));
-        ic->ttbc_d = ic->ampbc + 3 * nk2;
+        ic->ttbc_d = ic->ampbc + 4 * nk2;
       }
       // rho_bc feeds the masses; psi_bc only with the relative-velocity mode
       if ((rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->rho_bc))) return fail(rc);
       if (p->baryon_vrel && has_t && (rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->psi_bc)))
+        return fail(rc);
+      // the Eulerian branch of field output reads delta_bc without the relative-velocity amplitude
+      if (fields && p->baryon_vrel && (rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->rho_e)))
         return fail(rc);
     }
   }
@@ -1351,9 +1407,19 @@ extern "C" int mf_ic_run_species(mf_ic* ic, mf_particles* out, int nspecies) {
   if (!ic->p.baryons) return set_err(c, MF_ERR_ARG, "mf_ic_run_species: the pipeline has one species (use mf_ic_run)");
   if (!out || nspecies != 2) return set_err(c, MF_ERR_ARG, "mf_ic_run_species: two species expected");
   if (!ic->noise_set && !ic->noise_seeded) return set_err(c, MF_ERR_STATE, "mf_ic_run_species: white noise not set");
-  for (int sp = 0; sp < 2; ++sp)
-    if (out[sp].location == MF_LOC_HOST && (!out[sp].pos || !out[sp].vel || !out[sp].ids || !out[sp].mass))
-      return set_err(c, MF_ERR_ARG, "mf_ic_run_species: null host buffer");
+  const bool fields = ic->p.out_kind == MF_OUT_FIELDS;
+  // bytes handed over per species: pos, vel, ids, mass (field output: the
+  // dark matter's fields and mass field, the baryons' density and velocities)
+  const size_t n3 = (size_t)ic->p.ngrid * ic->p.ngrid * ic->p.ngrid;
+  const size_t bytes[2][4] = {{ic->pos_bytes, ic->vel_bytes, fields ? 0 : ic->id_bytes, ic->mass_bytes},
+                              {fields ? n3 * sizeof(double) : ic->pos_bytes, ic->vel_bytes, fields ? 0 : ic->id_bytes,
+                               fields ? 0 : ic->mass_bytes}};
+  for (int sp = 0; sp < 2; ++sp) {
+    if (out[sp].location != MF_LOC_HOST) continue;
+    void* const h[4] = {out[sp].pos, out[sp].vel, out[sp].ids, out[sp].mass};
+    for (int a = 0; a < 4; ++a)
+      if (bytes[sp][a] && !h[a]) return set_err(c, MF_ERR_ARG, "mf_ic_run_species: null host buffer");
+  }
   ic->early = nullptr;  // the hand-off happens after the run
   ic->early_all = false;
   ic->pos_early = false;
@@ -1367,9 +1433,8 @@ extern "C" int mf_ic_run_species(mf_ic* ic, mf_particles* out, int nspecies) {
     if (o.location == MF_LOC_HOST) {
       const void* src[4] = {dev.pos, dev.vel, dev.ids, dev.mass};
       void* dst[4] = {o.pos, o.vel, o.ids, o.mass};
-      const size_t bytes[4] = {ic->pos_bytes, ic->vel_bytes, ic->id_bytes, ic->mass_bytes};
       for (int a = 0; a < 4 && e == cudaSuccess; ++a)
-        e = cudaMemcpyAsync(dst[a], src[a], bytes[a], cudaMemcpyDeviceToHost, c->stream);
+        if (bytes[sp][a]) e = cudaMemcpyAsync(dst[a], src[a], bytes[sp][a], cudaMemcpyDeviceToHost, c->stream);
     } else {
       o = dev;
     }
@@ -1387,7 +1452,7 @@ extern "C" int mf_ic_mass_bytes(const mf_ic_params* p, size_t* bytes) {
   if (!bytes) return MF_ERR_ARG;
   int64_t np; size_t pb, vb, ib;
   output_sizes(p, &np, &pb, &vb, &ib);
-  *bytes = p->baryons ? (size_t)np * (p->pos64 ? 8 : 4) : 0;
+  *bytes = !p->baryons ? 0 : (size_t)np * ((p->pos64 || p->out_kind == MF_OUT_FIELDS) ? 8 : 4);
   return MF_OK;
 }
 

@@ -398,7 +398,7 @@ struct AssembleXInvOp {
     if (ch.nstep == 0) return v[0];
     C vm[1] = {mkc<T>(T(0), T(0))};
     if (kz == 0 || kz == (n >> 1)) vm[0] = assemble((n - i) % n, (n - j) % n, kz);
-    ch.apply<1>(n, i, j, kz, v, vm);
+    ch.template apply<1>(n, i, j, kz, v, vm);
     return v[0];
   }
   __device__ __forceinline__ void store(int j, int i, int kz, C v) const { dst[((long long)i * n + j) * Kz + kz] = v; }
@@ -516,7 +516,7 @@ struct Assemble3XInvOp {
     if (ch.nstep == 0) return;
     C vm[3];
     if (kz == 0 || kz == (n >> 1)) assemble((n - i) % n, (n - j) % n, kz, vm);
-    ch.apply<3>(n, i, j, kz, v, vm);
+    ch.template apply<3>(n, i, j, kz, v, vm);
   }
   __device__ __forceinline__ void store(int d, int j, int i, int kz, C v) const {
     dst[d][((long long)i * n + j) * Kz + kz] = v;

@@ -385,20 +385,36 @@ extern "C" int mf_ic_write_grafic2(mf_ic* ic, mf_grafic2* w) {
   // the plugin's units enter the fields (ic_generator.cc:815, :872-873)
   if (p->lunit != w->p.boxlen || p->vunit != w->p.boxlen)
     return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: pipeline units differ from the plugin's position/velocity unit");
-  mf_particles dev{};
-  dev.location = MF_LOC_DEVICE;
-  int rc = mf_ic_run(ic, &dev);
+  if (p->baryons && w->p.use_spt)
+    return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: Lagrangian baryon fields (grafic_use_SPT) are not built");
+  if (p->baryons && p->munit != 1.0 / w->p.Omega_m)
+    return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: pipeline mass unit differs from the plugin's (1 / Omega_m)");
+  mf_particles dev[2] = {};
+  dev[0].location = dev[1].location = MF_LOC_DEVICE;
+  int rc = p->baryons ? mf_ic_run_species(ic, dev, 2) : mf_ic_run(ic, &dev[0]);
   if (rc) return rc;
   const auto t0 = std::chrono::steady_clock::now();
   w->last_bytes = 0;
   w->last_kernel_ms = 0;
   const size_t n3 = (size_t)p->ngrid * p->ngrid * p->ngrid;
+  // dark matter (field_lagrangian): dx, dy, dz, vx, vy, vz and, with baryons,
+  // the mass field; baryons (field_eulerian, ic_generator.cc:766-789): the
+  // density and vx, vy, vz
+  struct Item { int species, comp; const double* src; };
+  Item items[11];
+  int ni = 0;
   static const int comp[6] = {MF_FC_DX, MF_FC_DY, MF_FC_DZ, MF_FC_VX, MF_FC_VY, MF_FC_VZ};
-  for (int k = 0; k < 6 && rc == MF_OK; ++k) {
-    const double* src = (k < 3 ? (const double*)dev.pos : (const double*)dev.vel) + (size_t)(k % 3) * n3;
-    rc = write_component(w, src, MF_PREC_F64, (size_t)p->ngrid, grafic_file_name(w, MF_SPECIES_DM, comp[k]),
-                         &w->last_bytes, &w->last_kernel_ms);
+  for (int k = 0; k < 6; ++k)
+    items[ni++] = {MF_SPECIES_DM, comp[k], (k < 3 ? (const double*)dev[0].pos : (const double*)dev[0].vel) + (size_t)(k % 3) * n3};
+  if (p->baryons) {
+    items[ni++] = {MF_SPECIES_DM, MF_FC_MASS, (const double*)dev[0].mass};
+    items[ni++] = {MF_SPECIES_BARYON, MF_FC_DENSITY, (const double*)dev[1].pos};
+    for (int k = 0; k < 3; ++k) items[ni++] = {MF_SPECIES_BARYON, comp[3 + k], (const double*)dev[1].vel + (size_t)k * n3};
   }
+  for (int k = 0; k < ni && rc == MF_OK; ++k)
+    if (!grafic_ignores(items[k].species, items[k].comp))
+      rc = write_component(w, items[k].src, MF_PREC_F64, (size_t)p->ngrid,
+                           grafic_file_name(w, items[k].species, items[k].comp), &w->last_bytes, &w->last_kernel_ms);
   w->last_wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return rc;
 }

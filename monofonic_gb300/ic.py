@@ -191,17 +191,29 @@ class ICGenerator:
 
     def run_species(self, to_host: bool = True):
         """two-species run (cfg.baryons): {"dm": (pos, vel, ids, mass),
-        "baryon": (...)} as numpy arrays, or device pointers"""
+        "baryon": (...)} as numpy arrays, or device pointers.  With field
+        output: dm = (displacements [3,n,n,n], velocities, None, mass field
+        [n,n,n]) and baryon = (density contrast [n,n,n], Eulerian velocities
+        [3,n,n,n], None, None) from the semiclassical branch."""
         outs = (L.mf_particles * 2)()
         keep = []
         if to_host:
             cfg = self.cfg
-            rt = np.float64 if cfg.pos64 else np.float32
+            n = cfg.ngrid
             for sp in range(2):
-                arrs = (np.empty((self.npart, 3), dtype=rt), np.empty((self.npart, 3), dtype=rt),
-                        np.empty(self.npart, dtype=np.uint64 if cfg.id64 else np.uint32), np.empty(self.npart, dtype=rt))
+                if cfg.out_kind == "fields":
+                    # dark matter: dx,dy,dz / vx,vy,vz grids and the mass field;
+                    # baryons (Eulerian branch): density contrast and vx,vy,vz
+                    arrs = ((np.empty((3, n, n, n)) if sp == 0 else np.empty((n, n, n))), np.empty((3, n, n, n)),
+                            None, np.empty((n, n, n)) if sp == 0 else None)
+                else:
+                    rt = np.float64 if cfg.pos64 else np.float32
+                    arrs = (np.empty((self.npart, 3), dtype=rt), np.empty((self.npart, 3), dtype=rt),
+                            np.empty(self.npart, dtype=np.uint64 if cfg.id64 else np.uint32),
+                            np.empty(self.npart, dtype=rt))
                 keep.append(arrs)
-                outs[sp].pos, outs[sp].vel, outs[sp].ids, outs[sp].mass = (a.ctypes.data for a in arrs)
+                outs[sp].pos, outs[sp].vel, outs[sp].ids, outs[sp].mass = (
+                    a.ctypes.data if a is not None else None for a in arrs)
                 outs[sp].location = L.MF_LOC_HOST
         else:
             for sp in range(2):

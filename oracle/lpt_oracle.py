@@ -784,6 +784,49 @@ def two_species_particles(f: LPTFields, L, order, cs, Omega_m, Omega_b, lattice=
     return out
 
 
+def _full_kgrids(n, L):
+    """get_k over a complex n^3 grid (grid_fft.hh:282-296): index > n/2 negative"""
+    idx = np.arange(n)
+    k = (idx - (idx > n // 2) * n) * (2.0 * math.pi / L)
+    return np.meshgrid(k, k, k, indexing="ij")
+
+
+def eulerian_fields(f: LPTFields, L, order, cs, C, Tdbc=None, vunit=1.0, Dplus_target=1.0):
+    """the semiclassical (PPT) Eulerian branch of a species
+    (ic_generator.cc:679-791): returns the density contrast |psi|^2 - 1 and
+    the three velocity components"""
+    n = f.phi.shape[0]
+    kx, ky, kz = kgrids(n, L)
+    kmod = np.sqrt(kx * kx + ky * ky + kz * kz)
+    a_d, _ = bc_amplitudes(kmod, cs, Tdbc, None, False, Dplus_target)
+    rk = f.wn * a_d
+    rk[0, 0, 0] = 0
+    prho = np.sqrt(1.0 + C * c2r(rk, n))
+    phi = c2r(f.phi, n)
+    d = np.abs(np.diff(phi, axis=0))  # base i in 0..n-2 (ic_generator.cc:704)
+    dy = np.abs(np.roll(phi, -1, axis=1) - phi)[:-1]
+    dz = np.abs(np.roll(phi, -1, axis=2) - phi)[:-1]
+    maxd = max(d.max(), dy.max(), dz.max())
+    D = cs.Dplus
+    hbar = maxd / math.pi / D * 1.01
+    phi2 = c2r(f.phi2, n) if order > 1 else None
+    arg = (phi + phi2) if order > 1 else phi
+    psi = prho * np.exp(1j * (1.0 / hbar) * arg / D)
+    K = _full_kgrids(n, L)
+    k2 = K[0] ** 2 + K[1] ** 2 + K[2] ** 2
+    psi = np.fft.ifftn(np.fft.fftn(psi, norm="ortho") * np.exp(-0.5j * hbar * k2 * D), norm="ortho")
+    if order > 1:
+        psi = psi * np.exp(1j * (1.0 / hbar) * phi2 / D)
+    rho = (psi.real ** 2 + psi.imag ** 2) - 1.0
+    vu = D * cs.vfac / L * vunit
+    psik = np.fft.fftn(psi, norm="ortho")
+    vel = []
+    for dd in range(3):
+        g = np.fft.ifftn(psik * (1j * K[dd]), norm="ortho")
+        vel.append(vu * np.real((np.conj(psi) * g - psi * np.conj(g)) / (2j / hbar)) / (1.0 + rho))
+    return rho, vel
+
+
 # ----------------------------------------------------------------------------
 # power spectrum (src/grid_fft.cc:1133-1210)
 # ----------------------------------------------------------------------------

@@ -18,8 +18,8 @@ def _tables(n, L):
     """smooth stand-ins for a Boltzmann code's T_delta_bc and T_theta_bc (the
     Eisenstein-Hu plugin returns zero for both), as callables of k and as the
     tables the library takes (k = sqrt(k2)*2pi/L)"""
-    Tdbc = lambda k: -0.08 * np.exp(-k / 0.7) / (1.0 + (k / 0.05) ** 2) ** 0.5
-    Ttbc = lambda k: 0.03 * np.exp(-k / 0.4) / (1.0 + (k / 0.1) ** 2)
+    Tdbc = lambda k: -0.01 * np.exp(-k / 0.7) / (1.0 + (k / 0.05) ** 2) ** 0.5
+    Ttbc = lambda k: 0.003 * np.exp(-k / 0.4) / (1.0 + (k / 0.1) ** 2)
     k = np.sqrt(np.arange(3 * (n // 2) ** 2 + 1, dtype=np.float64)) * (2 * math.pi / L)
     return Tdbc, Ttbc, Tdbc(k), Ttbc(k)
 
@@ -128,9 +128,9 @@ def test_two_species_errors(ctx):
     with pytest.raises(mf.MFError, match="run_species"):
         g.run()
     g.close()
-    with pytest.raises(mf.MFError):  # two-species field output is not built
+    with pytest.raises(mf.MFError):  # field output needs the SC lattice
         ic.ICGenerator(ctx, ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2, baryons=True, munit=1.0,
-                                        out_kind="fields"), sc)
+                                        out_kind="fields", lattice="bcc"), sc)
     with pytest.raises(mf.MFError):  # mass unit required
         ic.ICGenerator(ctx, ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2, baryons=True, munit=0.0), sc)
     one = ic.ICGenerator(ctx, ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2), sc)
@@ -138,3 +138,98 @@ def test_two_species_errors(ctx):
     with pytest.raises(mf.MFError, match="one species"):
         one.run_species()
     one.close()
+
+
+def _fields_run(ctx, n, L, z, order, prec, tables, vrel, munit=2.5, seed=21):
+    from monofonic_gb300 import ic
+    cosmo, sc, osc = setup(z)
+    noise = ic.white_noise(n, seed)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=order, precision=prec, lunit=L, vunit=L,
+                      out_kind="fields", baryons=True, baryon_vrel=vrel, munit=munit)
+    Tdbc = Ttbc = tdbc = ttbc = None
+    if tables:
+        Tdbc, Ttbc, tdbc, ttbc = _tables(n, L)
+    g = ic.ICGenerator(ctx, cfg, sc, tk_dbc=tdbc, tk_tbc=ttbc)
+    g.set_noise(noise)
+    got = g.run_species()
+    f = O.lpt_potentials(noise, L, order, osc)
+    lag = O.two_species_particles(f, L, order, osc, COSMO_KW["Omega_m"], COSMO_KW["Omega_b"], lattice=0, lunit=L,
+                                  vunit=L, munit=munit, Tdbc=Tdbc, Ttbc=Ttbc, vrel=vrel)
+    fb = COSMO_KW["Omega_b"] / COSMO_KW["Omega_m"]
+    eul = O.eulerian_fields(f, L, order, osc, 1.0 - fb, Tdbc=Tdbc, vunit=L)
+    return g, got, lag, eul
+
+
+@pytest.mark.parametrize("order,tables,vrel", [(1, True, False), (2, False, False), (2, True, True), (3, True, False)])
+def test_two_species_fields_f64(ctx, order, tables, vrel):
+    """field output with baryons: the dark matter's Lagrangian fields and mass
+    field, the baryons' semiclassical Eulerian density and velocities
+    (ic_generator.cc:679-791); the Eulerian fields to rel-L2 1e-10 (phases of
+    hundreds of radians)"""
+    n, L, z = 32, 50.0, 24.0
+    g, got, lag, eul = _fields_run(ctx, n, L, z, order, "f64", tables, vrel)
+    dx, vx, _, mass = got["dm"]
+    q = lattice_q(n, 0, L)
+    rpos, rvel, _, rmass = lag["dm"]
+    for d in range(3):
+        assert rel_l2(dx[d].reshape(-1), (rpos - q)[:, d]) < 1e-12
+        assert rel_l2(vx[d].reshape(-1), rvel[:, d]) < 1e-12
+    m0 = (COSMO_KW["Omega_m"] - COSMO_KW["Omega_b"]) * 2.5
+    rm = rmass * n ** 3  # the field is written as is, without pmeanmass
+    if tables:
+        assert rel_l2(mass.reshape(-1) - m0, rm - m0) < 1e-12
+    assert np.max(np.abs(mass.reshape(-1) - rm)) <= 1e-13 * m0
+    rho, vel = got["baryon"][0], got["baryon"][1]
+    rrho, rvel_e = eul
+    assert rel_l2(rho, rrho) < 1e-10
+    for d in range(3):
+        assert rel_l2(vel[d], rvel_e[d]) < 1e-10, d
+    assert np.abs(rrho).max() > 1e-3  # a non-trivial density field
+    g.close()
+
+
+def test_two_species_fields_f32(ctx):
+    """FP32-bulk pipeline: the Eulerian branch runs in FP64 from the FP32
+    potentials; the density error follows the potentials' rounding times the
+    phase (hundreds of radians), so its tolerance is 5e-3"""
+    n, L, z = 32, 50.0, 24.0
+    g, got, lag, eul = _fields_run(ctx, n, L, z, 3, "f32", True, True)
+    q = lattice_q(n, 0, L)
+    for d in range(3):
+        assert rel_l2(got["dm"][0][d].reshape(-1), (lag["dm"][0] - q)[:, d]) < 1e-5
+    assert rel_l2(got["baryon"][0], eul[0]) < 5e-3
+    for d in range(3):
+        assert rel_l2(got["baryon"][1][d], eul[1][d]) < 5e-3
+    g.close()
+
+
+def test_grafic2_two_species(ctx, tmp_path):
+    """the GRAFIC-2 plugin with baryons: dark matter dx..vz and mass, baryon
+    density and velocities; dark-matter density and baryon mass skipped"""
+    from monofonic_gb300 import ic
+    from monofonic_gb300.output import Grafic2Output
+    from oracle import grafic2_oracle as G
+    n, L, z = 32, 50.0, 24.0
+    cosmo, sc, osc = setup(z)
+    Om, Ob = COSMO_KW["Omega_m"], COSMO_KW["Omega_b"]
+    w = Grafic2Output(ctx, str(tmp_path / "ics"), n, L, z, 100 * COSMO_KW["h"], Om, 1 - Om, Ob, baryons=True)
+    assert "hydro=.true." in (tmp_path / "ics" / "ramses.nml").read_text()
+    Tdbc, Ttbc, tdbc, ttbc = _tables(n, L)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=2, lunit=w.position_unit(), vunit=w.velocity_unit(),
+                      out_kind="fields", baryons=True, munit=w.mass_unit())
+    gen = ic.ICGenerator(ctx, cfg, sc, tk_dbc=tdbc, tk_tbc=ttbc)
+    noise = ic.white_noise(n, 4)
+    gen.set_noise(noise)
+    w.write_ic(gen)
+    gen.set_noise(noise)
+    out = gen.run_species()
+    hdr = G.header(n, L, z, 100 * COSMO_KW["h"], Om, 1 - Om)
+    expect = {("dm", "dx"): out["dm"][0][0], ("dm", "vz"): out["dm"][1][2], ("dm", "mass"): out["dm"][3],
+              ("baryon", "density"): out["baryon"][0], ("baryon", "vy"): out["baryon"][1][1]}
+    for (sp, c), field in expect.items():
+        assert open(G.file_name(str(tmp_path / "ics"), sp, c), "rb").read() == G.file_bytes(field, hdr), (sp, c)
+    names = sorted(p.name for p in (tmp_path / "ics").iterdir())
+    assert names == sorted(["ramses.nml", "ic_poscx", "ic_poscy", "ic_poscz", "ic_velcx", "ic_velcy", "ic_velcz",
+                            "ic_massc", "ic_deltab", "ic_velbx", "ic_velby", "ic_velbz"])
+    gen.close()
+    w.close()
