@@ -44,6 +44,29 @@ __device__ __forceinline__ C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; 
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
 // multiply by -i (forward) or +i (inverse)
+// Float-pair ("double-float") arithmetic on the FP32 pipes, where GB300's
+// FP64 rate would bound a streaming kernel.  A double value v is carried as
+// the unevaluated pair (hi, lo) = (RN(v), RN(v - RN(v))), ~48 significant bits.
+// q + psi rounded to float for a pair q and a float psi: TwoSum of q.hi and
+// psi (exact), then the low parts; the result is the float nearest to the
+// exact sum except when that sum lies within ~2^-24 ulp of a tie.
+__device__ __forceinline__ float ff_add_q(float2 q, float psi) {
+  const float s = q.x + psi;
+  const float bb = s - q.x;
+  const float e = (q.x - (s - bb)) + (psi - bb);
+  return s + (e + q.y);
+}
+// accumulate w*x into the pair (h, l) for a pair weight (wh, wl) and a float x
+__device__ __forceinline__ void ff_axpy(float wh, float wl, float x, float& h, float& l) {
+  const float p = wh * x;
+  const float pe = fmaf(wl, x, fmaf(wh, x, -p));  // exact error of wh*x, plus wl*x
+  const float s = h + p;
+  const float bb = s - h;
+  const float e = (h - (s - bb)) + (p - bb);  // TwoSum error of h + p
+  h = s;
+  l = l + (e + pe);
+}
+
 template <bool INV, typename C>
 __device__ __forceinline__ C cmul_mi(C a) { C r; if (INV) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; } return r; }
 

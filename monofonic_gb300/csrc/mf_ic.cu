@@ -2,6 +2,7 @@
 // device: white noise -> phi(1) -> phi(2), phi(3), A(3) through the fused
 // Orszag convolver -> displacement/velocity assembly -> lattice positions,
 // velocities and particle IDs.
+#include <algorithm>
 #include <cmath>
 #include <initializer_list>
 #include <cstring>
@@ -178,6 +179,28 @@ __global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, con
                          const double* __restrict__ wbc = nullptr) {
   const double w1 = w[0], w2 = w[1], w3 = w[2];
   const double wb = pbc ? *wbc : 0.0;
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 grids: the weighted sum as a float pair, ~48 bits before the final
+    // rounding, on the FP32 pipes (the FP64 rate bounded this pass)
+    float wh[4], wl[4];
+    const double wd[4] = {w1, w2, w3, wb};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      wh[q] = __double2float_rn(wd[q]);
+      wl[q] = __double2float_rn(wd[q] - (double)wh[q]);
+    }
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+      const float2 a = p1[idx];
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      ff_axpy(wh[0], wl[0], a.x, rh, rl);
+      ff_axpy(wh[0], wl[0], a.y, ih, il);
+      if (p2) { const float2 b = p2[idx]; ff_axpy(wh[1], wl[1], b.x, rh, rl); ff_axpy(wh[1], wl[1], b.y, ih, il); }
+      if (p3) { const float2 c = p3[idx]; ff_axpy(wh[2], wl[2], c.x, rh, rl); ff_axpy(wh[2], wl[2], c.y, ih, il); }
+      if (pbc) { const float2 b = pbc[idx]; ff_axpy(wh[3], wl[3], b.x, rh, rl); ff_axpy(wh[3], wl[3], b.y, ih, il); }
+      out[idx] = make_float2(rh + rl, ih + il);
+    }
+    return;
+  }
   for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
     const cplx<T> a = p1[idx];
     double r = w1 * (double)a.x, im = w1 * (double)a.y;
@@ -195,12 +218,23 @@ __global__ void k_phitot(cplx<T>* out, const cplx<T>* p1, const cplx<T>* p2, con
 // q_d = (idx_d + s_d)/n * lunit (get_unit_r_shifted, grid_fft.hh:242-252)
 template <typename T, typename P>
 __global__ void k_lattice3(const T* psi0, const T* psi1, const T* psi2, int n, P* dst, int ishift,
-                           const double* __restrict__ q, int with_q, int fields_mode) {
+                           const double* __restrict__ q, int with_q, int fields_mode,
+                           const float2* __restrict__ qf = nullptr) {
   const size_t n3 = (size_t)n * n * n;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n3; c += (size_t)gridDim.x * blockDim.x) {
     const size_t line = c / n;
     const int k = (int)(c % n);
     const size_t off = line * (n + 2) + k;
+    if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
+      if (with_q && !fields_mode) {  // FP32 positions: q as a float pair (ff_add_q)
+        const int j = (int)(line % n), i = (int)(line / n);
+        P* o = dst + 3 * ((size_t)ishift * n3 + c);
+        o[0] = ff_add_q(qf[i], psi0[off]);
+        o[1] = ff_add_q(qf[n + j], psi1[off]);
+        o[2] = ff_add_q(qf[2 * n + k], psi2[off]);
+        continue;
+      }
+    }
     double v0 = (double)psi0[off], v1 = (double)psi1[off], v2 = (double)psi2[off];
     if (fields_mode) {
       dst[c] = (P)v0;
@@ -274,6 +308,21 @@ ShiftChain<T> lattice_chain(const void* phase, int lattice, bool secondary, int 
     for (int q = 0; q < 3; ++q)
       ch.s4[ch.nstep][q] = (int)lround(4 * (kShifts[lattice][st][q] - kShifts[lattice][st - 1][q]));
   return ch;
+}
+
+// device table of lattice coordinates: the doubles q[ishift][d][idx],
+// followed by the same values as float pairs (hi, lo) for FP32 positions
+cudaError_t upload_lattice_table(const std::vector<double>& q, double** out) {
+  std::vector<double> buf(2 * q.size());
+  std::copy(q.begin(), q.end(), buf.begin());
+  float2* qf = reinterpret_cast<float2*>(buf.data() + q.size());
+  for (size_t i = 0; i < q.size(); ++i) {
+    const float hi = (float)q[i];
+    qf[i] = make_float2(hi, (float)(q[i] - (double)hi));
+  }
+  cudaError_t e = cudaMalloc(out, buf.size() * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpy(*out, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice);
+  return e;
 }
 
 }  // namespace
@@ -782,6 +831,7 @@ int enqueue_impl(mf_ic* ic) {
     }
     void* dst = sp ? (vel ? ic->bvel : ic->bpos) : (vel ? ic->dvel : ic->dpos);
     const double* qbase = sp ? ic->bqtab : ic->qtab;
+    const float2* qfbase = reinterpret_cast<const float2*>(qbase + (size_t)overload * 3 * n);
     const bool three = Launch<T>::assemble3_supported(n);
     for (int ish = 0; ish < overload; ++ish) {
       if (three) {  // x pass of the three components in one launch
@@ -852,6 +902,7 @@ int enqueue_impl(mf_ic* ic) {
         for (int d = 0; d < 3; ++d) la.comp[d] = ic->tmp[d]->d;
         la.dst = dst;
         la.q = qt;
+        la.qf = qfbase + (size_t)ish * 3 * n;
         la.n = n;
         la.nlines = n * n;
         la.ishift = fields ? 0 : ish;
@@ -878,7 +929,8 @@ int enqueue_impl(mf_ic* ic) {
       else if (p.pos64)
         k_lattice3<T, double><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (double*)dst, ish, qt, vel ? 0 : 1, 0);
       else
-        k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, qt, vel ? 0 : 1, 0);
+        k_lattice3<T, float><<<blocks_for(n3), kThreads, 0, s>>>(q0, q1, q2, n, (float*)dst, ish, qt, vel ? 0 : 1, 0,
+                                                                 qfbase + (size_t)ish * 3 * n);
       CK(cudaGetLastError());
       if (ic->early && !fields && MF_STREAM_HANDOFF) {
         const size_t slice = (vel ? ic->vel_bytes : ic->pos_bytes) / overload;
@@ -1138,9 +1190,8 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
       for (int d = 0; d < 3; ++d)
         for (int i = 0; i < n; ++i)
           q[((size_t)ish * 3 + d) * n + i] = ((double)i + kShifts[p->lattice][ish][d]) / (double)n * p->lunit;
-    e2 = cudaMalloc(&ic->qtab, q.size() * sizeof(double));
-    if (e2 == cudaSuccess) e2 = cudaMemcpy(ic->qtab, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice);
-    if (e2 != cudaSuccess) return fail(cuda_err(c, e2, "mf_ic_create: lattice table"));
+    if ((e2 = upload_lattice_table(q, &ic->qtab)) != cudaSuccess)
+      return fail(cuda_err(c, e2, "mf_ic_create: lattice table"));
   }
   if (p->plt) {
     PLTTables t;
@@ -1246,8 +1297,7 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
         for (int i = 0; i < n; ++i)
           q[((size_t)ish * 3 + d) * n + i] =
               ((double)i + (kShifts[p->lattice][ish][d] + kSecondShift[p->lattice][d])) / (double)n * p->lunit;
-    if ((e = cudaMalloc(&ic->bqtab, q.size() * sizeof(double))) != cudaSuccess ||
-        (e = cudaMemcpy(ic->bqtab, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = upload_lattice_table(q, &ic->bqtab)) != cudaSuccess)
       return fail(cuda_err(c, e, "mf_ic_create: secondary lattice table"));
     const bool has_d = p->tk_dbc_table != nullptr;
     const bool has_t = p->tk_tbc_table != nullptr;

@@ -312,6 +312,17 @@ __global__ void __launch_bounds__(NT) k_zc2r3_lattice(Lattice3Args a, const cplx
         for (int d = 0; d < 3; ++d) o[d] = (P)((h ? v[d][s].y : v[d][s].x) * T(a.norm));
         continue;
       }
+      if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
+        if (a.with_q && !a.fields_mode) {
+          // FP32 positions q + Psi with q as a float pair: the correctly
+          // rounded sum on the FP32 pipes (ff_add_q)
+          P* o = reinterpret_cast<P*>(a.dst) + 3 * ((long long)a.ishift * n3 + c);
+          const int qi[3] = {i, n + j, 2 * n + k};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) o[d] = ff_add_q(a.qf[qi[d]], (h ? v[d][s].y : v[d][s].x) * T(a.norm));
+          continue;
+        }
+      }
       double val[3];
       // normalised in the grid precision, as the component grids of the per-component path
 #pragma unroll

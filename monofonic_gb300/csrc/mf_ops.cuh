@@ -528,6 +528,7 @@ struct Lattice3Args {
   const void* comp[3];
   void* dst;
   const double* q;  // q[d*n + idx_d], lattice coordinates times the unit
+  const float2* qf; // the same as float pairs (hi, lo) for FP32 positions
   int n, nlines, ishift, with_q, fields_mode;
   double norm;      // 1/sqrt(n^3) of the c2r
 };
