@@ -270,32 +270,12 @@ __global__ void __launch_bounds__(NT) k_zc2r(OP op, const cplx<T>* __restrict__ 
 // grids of doubles.  Inputs: the three component grids after their x and y
 // passes, [line][n/2+1] complex.
 // ---------------------------------------------------------------------------
-template <typename T, int H, int NT, typename P>
-__global__ void __launch_bounds__(NT) k_zc2r3_lattice(Lattice3Args a, const cplx<T>* __restrict__ twH,
-                                                       const cplx<T>* __restrict__ twM) {
+// the lattice readout of one transformed line (particle ip = ishift*n^3 + cell)
+template <typename T, int H, typename P>
+__device__ __forceinline__ void lattice_line_out(Lattice3Args a, int line, int t,
+                                                 const cplx<T> (&v)[3][LineFFT<T, H, true>::E]) {
   using F = LineFFT<T, H, true>;
-  using C = cplx<T>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int t = threadIdx.x, ly = threadIdx.y;
-  const int line = blockIdx.x * blockDim.y + ly;
-  const bool valid = line < a.nlines;
-  const int n = a.n, Kz = H + 1;
-  C* sm[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    sm[d] = reinterpret_cast<C*>(smem_raw) + (ly * 3 + d) * (H + 1);
-    const C* src = reinterpret_cast<const C*>(a.comp[d]) + (long long)(valid ? line : 0) * Kz;
-    for (int k = t; k <= H; k += F::TPL) sm[d][k] = valid ? src[k] : mkc<T>(T(0), T(0));
-  }
-  __syncthreads();
-  C v[3][F::E];
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-#pragma unroll
-    for (int s = 0; s < F::E; ++s) v[d][s] = c2r_pre<T, H>(sm[d], F::in_index(t, s), twM);
-#pragma unroll
-  for (int d = 0; d < 3; ++d) F::run(v[d], t, sm[d], 1, twH, SyncBlock{});
-  if (!valid) return;
+  const int n = a.n;
   const long long n3 = (long long)n * n * n;
   const int i = line / n, j = line % n;
 #pragma unroll
@@ -343,6 +323,63 @@ __global__ void __launch_bounds__(NT) k_zc2r3_lattice(Lattice3Args a, const cplx
       }
     }
   }
+}
+
+
+template <typename T, int H, int LPB, typename P>
+__global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H, true>::E <= 8) ? 2 : 1)
+    k_zc2r3_lattice(Lattice3Args a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
+  using F = LineFFT<T, H, true>;
+  using C = cplx<T>;
+  constexpr int SL = 3 * (H + 1);  // complex values of one line's three components
+  // persistent CTAs over batches of LPB lines; the next batch is copied into
+  // the other shared-memory buffer (cp.async) while this one is transformed
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + LPB * SL;
+  const int t = threadIdx.x, ly = threadIdx.y;
+  const int tid = ly * F::TPL + t;
+  const int n = a.n, Kz = H + 1;
+  const int nb = (a.nlines + LPB - 1) / LPB;
+  auto issue = [&](int bt, C* buf) {
+    for (int q = tid; q < LPB * SL; q += LPB * F::TPL) {
+      const int l = q / SL, rem = q - l * SL, d = rem / Kz, k = rem - d * Kz;
+      const int line = bt * LPB + l;
+      if (line < a.nlines) {
+        const void* base = (d == 0) ? a.comp[0] : ((d == 1) ? a.comp[1] : a.comp[2]);
+        const C* g = reinterpret_cast<const C*>(base) + (long long)line * Kz + k;
+        if constexpr (sizeof(C) == 16) cp_async16(buf + q, g); else cp_async8(buf + q, g);
+      } else {
+        buf[q] = mkc<T>(T(0), T(0));
+      }
+    }
+    cp_async_commit();
+  };
+  int bt = blockIdx.x;
+  if (bt < nb) issue(bt, buf0); else cp_async_commit();
+  for (int it = 0; bt < nb; bt += gridDim.x, ++it) {
+    C* cur = (it & 1) ? buf1 : buf0;
+    C* nxt = (it & 1) ? buf0 : buf1;
+    const int bn = bt + gridDim.x;
+    if (bn < nb) issue(bn, nxt); else cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();  // every thread's copies of this batch have landed
+    const int line = bt * LPB + ly;
+    const bool valid = line < a.nlines;
+    C* sm[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sm[d] = cur + ly * SL + d * Kz;
+    C v[3][F::E];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) v[d][s] = c2r_pre<T, H>(sm[d], F::in_index(t, s), twM);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) F::run(v[d], t, sm[d], 1, twH, SyncBlock{});
+    if (valid) lattice_line_out<T, H, P>(a, line, t, v);
+    __syncthreads();  // cur is refilled by the next iteration's copies
+  }
+  cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------

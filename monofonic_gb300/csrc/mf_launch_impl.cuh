@@ -293,22 +293,30 @@ cudaError_t Launch<T>::assemble3_xinv(int L, Assemble3XInvOp<T> op, int nslab, i
 template <typename T, int H>
 cudaError_t launch_zc2r3_lattice(const Lattice3Args& a, bool p64, const cplx<T>* twH, const cplx<T>* twM,
                                  cudaStream_t s) {
-  constexpr int LPB = z_lpb<T, H, 3 * (H + 1)>();
+  // lines per batch: at most 256 threads, two batch buffers within ~100 KB so
+  // that two CTAs share an SM
   constexpr int TPL = LineFFT<T, H, true>::TPL;
-  const size_t smem = (size_t)LPB * 3 * (H + 1) * sizeof(cplx<T>);
-  dim3 block(TPL, LPB), grid((a.nlines + LPB - 1) / LPB);
-  if (p64) {
-    auto kern = k_zc2r3_lattice<T, H, TPL * LPB, double>;
+  constexpr int LPB = [] {
+    int l = 256 / TPL;
+    if (l < 1) l = 1;
+    while (l > 1 && 2 * (size_t)l * 3 * (H + 1) * sizeof(cplx<T>) > 100 * 1024) l /= 2;
+    return l;
+  }();
+  const size_t smem = (size_t)2 * LPB * 3 * (H + 1) * sizeof(cplx<T>);
+  const int nb = (a.nlines + LPB - 1) / LPB;
+  auto go = [&](auto kern) -> cudaError_t {
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, block, smem, s>>>(a, twH, twM);
-  } else {
-    auto kern = k_zc2r3_lattice<T, H, TPL * LPB, float>;
-    cudaError_t e = set_smem(kern, smem);
+    int per_sm = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPL * LPB, smem);
     if (e != cudaSuccess) return e;
-    kern<<<grid, block, smem, s>>>(a, twH, twM);
-  }
-  return cudaGetLastError();
+    const int grid = std::max(1, std::min(nb, std::max(1, per_sm) * nsm));
+    kern<<<grid, dim3(TPL, LPB), smem, s>>>(a, twH, twM);
+    return cudaGetLastError();
+  };
+  return p64 ? go(k_zc2r3_lattice<T, H, LPB, double>) : go(k_zc2r3_lattice<T, H, LPB, float>);
 }
 template <typename T>
 cudaError_t Launch<T>::z_c2r3_lattice(int H, const Lattice3Args& a, bool p64, const cplx<T>* twH,
