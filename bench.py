@@ -149,7 +149,7 @@ def algorithmic_bytes_ic(n: int, prec_bytes: int, overload: int = 2, plt: bool =
         # PLT table of 4 reals per mode, three outputs), component y passes
         "fft_col": 2 * 2 * S_NK + 2 * overload * ((1 + 3 + 3) * S_NK + (2 * S_NK if plt else 0))
                    + 2 * overload * 3 * 2 * S_NK,
-        # source products (7 + 10 + 21 real fields), two FP64 order sums (3 in, 1 out), ids
+        # source products (7 + 10 + 21 real fields), two order sums (3 in, 1 out), ids
         "pointwise": (7 + 10 + 21) * S_R + 2 * 4 * S_NK + npart * 8,
     }
     return out
@@ -629,7 +629,7 @@ def run_mf(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": (f"3LPT BCC 2x{n}^3 particles, Orszag 3/2 (M={3 * n // 2}), L=1000 Mpc/h, z=24, "
-                                    "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with FP64 order sum and q+Psi"),
+                                    "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with float-pair (~48-bit) order sum and q+Psi"),
                        "plt": True, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"},
             "latency_ms": {"p50": p50, "p99": p99},
             "gpu_launches": launches,
