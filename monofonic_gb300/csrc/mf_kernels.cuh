@@ -278,6 +278,33 @@ __device__ __forceinline__ void lattice_line_out(Lattice3Args a, int line, int t
   const int n = a.n;
   const long long n3 = (long long)n * n * n;
   const int i = line / n, j = line % n;
+  if constexpr (std::is_same<P, float>::value && std::is_same<T, float>::value) {
+    if (!a.fields_mode) {
+      // FP32 particles: the two particles 2m, 2m+1 of a slot are 24 contiguous
+      // bytes (8-byte aligned for even n), stored as three float2
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) {
+        const int m = F::out_index(t, s);
+        float w[6];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int k = 2 * m + h;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const float x = (h ? v[d][s].y : v[d][s].x) * T(a.norm);
+            const int qi = (d == 0) ? i : ((d == 1) ? n + j : 2 * n + k);
+            w[3 * h + d] = a.with_q ? ff_add_q(a.qf[qi], x) : x;
+          }
+        }
+        float2* o = reinterpret_cast<float2*>(reinterpret_cast<float*>(a.dst) +
+                                              3 * ((long long)a.ishift * n3 + (long long)line * n + 2 * m));
+        o[0] = make_float2(w[0], w[1]);
+        o[1] = make_float2(w[2], w[3]);
+        o[2] = make_float2(w[4], w[5]);
+      }
+      return;
+    }
+  }
 #pragma unroll
   for (int s = 0; s < F::E; ++s) {
     const int m = F::out_index(t, s);
@@ -341,17 +368,18 @@ __global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H,
   const int tid = ly * F::TPL + t;
   const int n = a.n, Kz = H + 1;
   const int nb = (a.nlines + LPB - 1) / LPB;
-  auto issue = [&](int bt, C* buf) {
-    for (int q = tid; q < LPB * SL; q += LPB * F::TPL) {
-      const int l = q / SL, rem = q - l * SL, d = rem / Kz, k = rem - d * Kz;
-      const int line = bt * LPB + l;
-      if (line < a.nlines) {
-        const void* base = (d == 0) ? a.comp[0] : ((d == 1) ? a.comp[1] : a.comp[2]);
-        const C* g = reinterpret_cast<const C*>(base) + (long long)line * Kz + k;
-        if constexpr (sizeof(C) == 16) cp_async16(buf + q, g); else cp_async8(buf + q, g);
-      } else {
-        buf[q] = mkc<T>(T(0), T(0));
-      }
+  // a batch of one component is LPB consecutive lines, contiguous in global
+  // memory: staged as [d][l][k] with 16-byte copies (an even LPB keeps both
+  // ends 16-byte aligned)
+  static_assert(LPB % 2 == 0, "even lines per batch");
+  constexpr int U = LPB * Kz * (int)sizeof(C) / 16;  // 16-byte units per component
+  auto issue = [&](int bt, C* buf) {  // nlines is a multiple of LPB (checked at launch)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const void* base = (d == 0) ? a.comp[0] : ((d == 1) ? a.comp[1] : a.comp[2]);
+      const char* g = reinterpret_cast<const char*>(base) + (size_t)bt * LPB * Kz * sizeof(C);
+      char* sb = reinterpret_cast<char*>(buf + d * LPB * Kz);
+      for (int u = tid; u < U; u += LPB * F::TPL) cp_async16(sb + 16 * u, g + 16 * u);
     }
     cp_async_commit();
   };
@@ -368,7 +396,7 @@ __global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H,
     const bool valid = line < a.nlines;
     C* sm[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) sm[d] = cur + ly * SL + d * Kz;
+    for (int d = 0; d < 3; ++d) sm[d] = cur + d * LPB * Kz + ly * Kz;
     C v[3][F::E];
 #pragma unroll
     for (int d = 0; d < 3; ++d)

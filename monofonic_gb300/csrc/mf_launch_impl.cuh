@@ -303,7 +303,8 @@ cudaError_t launch_zc2r3_lattice(const Lattice3Args& a, bool p64, const cplx<T>*
     return l;
   }();
   const size_t smem = (size_t)2 * LPB * 3 * (H + 1) * sizeof(cplx<T>);
-  const int nb = (a.nlines + LPB - 1) / LPB;
+  if (a.nlines % LPB) return cudaErrorInvalidValue;  // whole batches (n^2 lines, n even)
+  const int nb = a.nlines / LPB;
   auto go = [&](auto kern) -> cudaError_t {
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
