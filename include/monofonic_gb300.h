@@ -137,6 +137,9 @@ int mf_grid_shift(mf_grid* g, const double s[3], int transform_back);
  * *nbins receives int(kmax/kmin) */
 int mf_grid_power_spectrum(mf_grid* g, double* bin_k, double* bin_P, double* bin_eP,
                            int64_t* bin_count, int nbins_cap, int* nbins);
+/* Write_PowerSpectrum (src/grid_fft.cc:1104-1131): the same bins written as
+ * text, a header line and one line per non-empty bin (k, P, err, #modes) */
+int mf_grid_write_power_spectrum(mf_grid* g, const char* path);
 /* Grid_FFT<ccomplex_t> transforms (src/grid_fft.cc:56-63, FFTW_FORWARD /
  * FFTW_BACKWARD, unitary): in place on an n^3 complex FP64 device array
  * [i][j][k] on the context's stream (asynchronous) */

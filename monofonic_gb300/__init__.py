@@ -190,6 +190,10 @@ class Grid_FFT:
         m = nb.value
         return k[:m], P[:m], eP[:m], cnt[:m]
 
+    def Write_PowerSpectrum(self, ofname: str):
+        """Write_PowerSpectrum (grid_fft.cc:1104-1131): the binned P(k) as text"""
+        _check(self.ctx.ptr, lib().mf_grid_write_power_spectrum(self.ptr, ofname.encode()))
+
     def close(self):
         if getattr(self, "ptr", None):
             lib().mf_grid_destroy(self.ptr)

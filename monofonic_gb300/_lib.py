@@ -58,6 +58,7 @@ SIGNATURES = {
     "mf_grid_inverse_laplacian": (C.c_int, [C.c_void_p]),
     "mf_grid_shift": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int]),
     "mf_cgrid_fft": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "mf_grid_write_power_spectrum": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mf_grid_power_spectrum": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int)]),
     "mf_conv_create": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),

@@ -1,5 +1,6 @@
 // C ABI of libmfgpu: context, Grid_FFT and convolver handles.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -565,6 +566,24 @@ extern "C" int mf_grid_power_spectrum(mf_grid* g, double* bin_k, double* bin_P, 
     }
   }
   return MF_OK;
+}
+
+extern "C" int mf_grid_write_power_spectrum(mf_grid* g, const char* path) {
+  if (!g || !path) return MF_ERR_ARG;
+  const int cap = g->n;  // int(kmax / kmin) = n/2 bins
+  std::vector<double> k(cap), P(cap), eP(cap);
+  std::vector<int64_t> cnt(cap);
+  int nb = 0;
+  int rc = mf_grid_power_spectrum(g, k.data(), P.data(), eP.data(), cnt.data(), cap, &nb);
+  if (rc) return rc;
+  FILE* fp = std::fopen(path, "w");
+  if (!fp) return set_err(g->ctx, MF_ERR_IO, std::string("mf_grid_write_power_spectrum: cannot create ") + path);
+  // the reference streams with setw and the default float format (%g)
+  bool ok = std::fprintf(fp, "# %14s%16s%16s%16s\n", "k", "P(k)", "err. P(k)", "#modes") > 0;
+  for (int b = 0; b < nb && ok; ++b)
+    if (cnt[b] > 0) ok = std::fprintf(fp, "%16g%16g%16g%16lld\n", k[b], P[b], eP[b], (long long)cnt[b]) > 0;
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? MF_OK : set_err(g->ctx, MF_ERR_IO, std::string("mf_grid_write_power_spectrum: write failed on ") + path);
 }
 
 // ---------------------------------------------------------------------------

@@ -71,3 +71,30 @@ def test_complex_grid_fft_matches_numpy(ctx, n):
     assert mf.lib().mf_cgrid_fft(ctx.ptr, t.data_ptr(), n, 1) == 0
     ctx.synchronize()
     assert np.linalg.norm(t.cpu().numpy() - a) / np.linalg.norm(a) < 1e-13
+
+
+@pytest.mark.gpu
+def test_power_spectrum_and_its_file(ctx, tmp_path):
+    """Compute_PowerSpectrum (grid_fft.cc:1133-1210) against the oracle, and
+    Write_PowerSpectrum (grid_fft.cc:1104-1131): header and one line per
+    non-empty bin, values in the default stream format (6 significant digits)"""
+    import monofonic_gb300 as mf
+    n, L = 32, 100.0
+    x = O.white_noise(n, 3)
+    g = mf.Grid_FFT(ctx, n, L)
+    g.set_real(x)
+    k, P, eP, c = g.Compute_PowerSpectrum()
+    rk, rP, reP, rc = O.power_spectrum(O.r2c(x), L)
+    assert np.array_equal(c, rc)
+    assert np.allclose(k, rk, rtol=1e-12, atol=0)
+    assert np.allclose(P, rP, rtol=1e-10, atol=0)
+    assert np.allclose(eP, reP, rtol=1e-8, atol=0)
+    path = tmp_path / "input_powerspec.txt"
+    g.Write_PowerSpectrum(str(path))
+    lines = path.read_text().splitlines()
+    assert lines[0] == "# " + "k".rjust(14) + "P(k)".rjust(16) + "err. P(k)".rjust(16) + "#modes".rjust(16)
+    rows = np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
+    m = c > 0
+    assert rows.shape == (m.sum(), 4) and all(len(ln) == 64 for ln in lines[1:])
+    assert np.allclose(rows[:, 0], k[m], rtol=1e-5) and np.allclose(rows[:, 1], P[m], rtol=1e-5)
+    assert np.array_equal(rows[:, 3].astype(np.int64), c[m])
