@@ -107,7 +107,9 @@ __global__ void k_pk(const cplx<T>* d, int n, double kfac, int nbins, double* ac
     const int j = (int)((idx / Kz) % n);
     const int i = (int)(idx / ((size_t)Kz * n));
     const double kx = kcomp<double>(i, n, kfac), ky = kcomp<double>(j, n, kfac), kk = kcomp<double>(kz, n, kfac);
-    const double k = sqrt(kx * kx + ky * ky + kk * kk);
+    // |k| without contraction into FMAs (modes of integer norm sit on bin
+    // edges, so the bin follows the exact rounding of x*x + y*y + z*z)
+    const double k = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kk, kk)));
     if (k >= kmin && k < kmax) {
       const int b = (int)(k / dk);
       const cplx<T> z = d[idx];
