@@ -573,6 +573,8 @@ int shared_sources(mf_ic* ic, bool timed) {
     T* outs[kSrcOutputs] = {};
     for (int o = 0; o < kSrcOutputs; ++o)
       if (P0 + o < ((p.lpt_order > 2) ? 22 : 7)) outs[o] = (T*)R(P0 + o);
+    if (set == SRC_PHI2_PAIRS)  // the pairs go to the (still unused) slots of the phi(2) Hessians
+      for (int o = 1; o < 6; ++o) outs[o] = (T*)R(5 + o);
     LaunchScope ls(c, KK_POINTWISE);
     return pw_sources<T>(set, fields, outs, 2 * rl, s);
   };
@@ -597,19 +599,20 @@ int shared_sources(mf_ic* ic, bool timed) {
   };
 
   // ---- phi(2) (ic_generator.cc:471-488) ----------------------------------
+  // with 3LPT the convolve3 first stages (truncated pair products phi,00 phi,11
+  // / phi,01 phi,02 / phi,12^2 / phi,02^2 / phi,01^2) come out of the same pass
   CK(hessians(0, 0));
-  CK(sources(SRC_PHI2));
+  mf_grid* qg[5] = {ic->tmp[0], ic->tmp[1], ic->tmp[2], ic->wn, ic->qx};
+  CK(sources(p.lpt_order > 2 ? SRC_PHI2_PAIRS : SRC_PHI2));
   CK(r2c_unpad(P0, (cplx<T>*)ic->f[1]->d, OUT_ASSIGN, 1));
   ic->f[1]->space = MF_SPACE_K;
+  if (p.lpt_order > 2)
+    for (int k = 0; k < 5; ++k) CK(r2c_unpad(6 + k, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
   if (timed) CK(cudaEventRecord(ic->ev[2], s));
   if (p.lpt_order > 2) {
     // ---- phi(3) (ic_generator.cc:511-528) --------------------------------
     CK(hessians(1, 6));
-    // convolve3 first stages: truncated pair products phi,00 phi,11 / phi,01 phi,02 /
-    // phi,12^2 / phi,02^2 / phi,01^2, then their padded c2r
-    mf_grid* qg[5] = {ic->tmp[0], ic->tmp[1], ic->tmp[2], ic->wn, ic->qx};
-    CK(sources(SRC_PAIRS));
-    for (int k = 0; k < 5; ++k) CK(r2c_unpad(P0 + k, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
+    // the pairs' padded c2r
     {
       Operand<T> ops[3];
       int dst[3];

@@ -104,9 +104,10 @@ template <typename T> cudaError_t pw_shift(cplx<T>* d, int n, double kfac, doubl
 template <typename T> cudaError_t pw_fill_from_f64(T* d, const double* src, int n, cudaStream_t s);
 // LPT source products over the shared padded real fields (mf_sources.cu):
 // fields[0..16] (Hessians of phi, of phi(2), convolve3 pair products), outs
-// the product sums of the set: SRC_PHI2 1, SRC_PAIRS 5, SRC_PHI3_A3 4
-enum { SRC_PHI2 = 0, SRC_PAIRS = 1, SRC_PHI3_A3 = 2 };
-constexpr int kSrcFields = 17, kSrcOutputs = 5;
+// the product sums of the set: SRC_PHI2 1, SRC_PAIRS 5, SRC_PHI3_A3 4,
+// SRC_PHI2_PAIRS 6 (the phi(2) source and the five pairs in one pass)
+enum { SRC_PHI2 = 0, SRC_PAIRS = 1, SRC_PHI3_A3 = 2, SRC_PHI2_PAIRS = 3 };
+constexpr int kSrcFields = 17, kSrcOutputs = 6;
 template <typename T>
 cudaError_t pw_sources(int set, const T* const* fields, T* const* outs, size_t n, cudaStream_t s);
 

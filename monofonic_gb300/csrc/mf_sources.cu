@@ -35,6 +35,13 @@ struct SrcSetPhi2 {
 struct SrcSetPairs {
   static constexpr SrcTerm terms[] = {{0, 0, 1, 1.0}, {1, 3, 4, 1.0}, {2, 5, 5, 1.0}, {3, 4, 4, 1.0}, {4, 3, 3, 1.0}};
 };
+// the phi(2) source (output 0) and the five convolve3 pairs (outputs 1..5):
+// both read only the Hessians of phi, so one pass serves a 3LPT run
+struct SrcSetPhi2Pairs {
+  static constexpr SrcTerm terms[] = {{0, 0, 1, 1.0},  {0, 0, 2, 1.0},  {0, 1, 2, 1.0},  {0, 3, 3, -1.0},
+                                      {0, 4, 4, -1.0}, {0, 5, 5, -1.0}, {1, 0, 1, 1.0},  {2, 3, 4, 1.0},
+                                      {3, 5, 5, 1.0},  {4, 4, 4, 1.0},  {5, 3, 3, 1.0}};
+};
 // phi(3) (output 0) and A(3) x, y, z (outputs 1..3)
 #define MF_A3_TERMS(d)                                                                                       \
   {1 + d, 6 + src_hx(d, src_dp(d)), src_hx(d, src_dpp(d)), 1.0},                                             \
@@ -162,6 +169,7 @@ cudaError_t pw_sources(int set, const T* const* fields, T* const* outs, size_t n
     case SRC_PHI2: return launch_sources<T, SrcSetPhi2>(fields, outs, n, s);
     case SRC_PAIRS: return launch_sources<T, SrcSetPairs>(fields, outs, n, s);
     case SRC_PHI3_A3: return launch_sources<T, SrcSetPhi3A3>(fields, outs, n, s);
+    case SRC_PHI2_PAIRS: return launch_sources<T, SrcSetPhi2Pairs>(fields, outs, n, s);
     default: return cudaErrorInvalidValue;
   }
 }
