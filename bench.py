@@ -210,6 +210,13 @@ def cpu_sample(n: int, threads: int):
             "seconds_per_ic": t_ic}
 
 
+def workload_config(n, world):
+    """the workload both arms report"""
+    return {"workload": (f"3LPT BCC 2x{n}^3 particles, Orszag 3/2 (M={3 * n // 2}), L=1000 Mpc/h, z=24, "
+                         "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with float-pair (~48-bit) order sum and q+Psi"),
+            "plt": True, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -226,7 +233,8 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"3LPT BCC 2x{n}^3, Orszag M={3 * n // 2}, L=1000, z=24", "impl": "oracle port"},
+            "config": workload_config(n, 1) | {"reference_impl": "oracle port (numpy/scipy FP64 restatement of the "
+                                                                  "reference, which cannot be built here)"},
             "impl": "reference",
             "cpu_baseline": {k: vals[-1][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": UNIT},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -628,9 +636,7 @@ def run_mf(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": (f"3LPT BCC 2x{n}^3 particles, Orszag 3/2 (M={3 * n // 2}), L=1000 Mpc/h, z=24, "
-                                    "Eisenstein-Hu, seeded N(0,1) noise; FP32-bulk with float-pair (~48-bit) order sum and q+Psi"),
-                       "plt": True, "l2": "inputs larger than L2 (working set > 16 GB)", "parallelism": f"replicas x{world}"},
+            "config": workload_config(n, world),
             "latency_ms": {"p50": p50, "p99": p99},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
