@@ -382,7 +382,6 @@ struct mf_ic {
   bool shared = false;
   void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last 5 or 1: product sums)
   void* w3 = nullptr;   // three work buffers [M][M][N/2+1] complex
-  mf_grid* qx = nullptr;  // fifth N-grid buffer of the phi(3) pair products
 };
 
 namespace {
@@ -598,35 +597,77 @@ int shared_sources(mf_ic* ic, bool timed) {
     return cudaSuccess;
   };
 
+  // convolve3's first stage for one pair product held as a padded real field:
+  // r2c, the truncation to the N-cube (unpad with the Nyquist planes zeroed,
+  // convolution.hh:543-549, :618-653) and the padded c2r of the truncated
+  // field (pad_insert, :570-592) into another real field.  The x passes of
+  // the two transforms and the truncation are one pass (ConvXTruncOp), so the
+  // unpadded N-grid never goes to HBM.
+  auto truncate_pair = [&](int src, int dstf) -> cudaError_t {
+    cudaError_t e2;
+    ZConvArgs<T> za{};
+    za.in[0] = R(src);
+    za.out = W[0];
+    za.nop = 1;
+    za.kin = H;
+    za.kout = Kz;
+    za.in_stride = H;
+    za.out_stride = Kz;
+    za.nlines = M * M;
+    za.out_scale = T(1);
+    za.err = c->d_err;
+    {
+      LaunchScope ls(c, KK_CONV_Z);
+      if ((e2 = Launch<T>::z_r2c_tma(H, za, twH, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvYFwdOp<T> yf{W[0], W[0], g};
+    {
+      LaunchScope ls(c, KK_CONV_YFWD);
+      if ((e2 = Launch<T>::conv_yfwd(M, yf, M, Kz, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvXTruncOp<T> xt{W[0], g, scale_out, scale_in};
+    {
+      LaunchScope ls(c, KK_CONV_XFWD);
+      if ((e2 = Launch<T>::conv_xtrunc(M, xt, N, Kz, twM, s)) != cudaSuccess) return e2;
+    }
+    ConvYInvOp<T> yo{};
+    yo.src[0] = W[0];
+    yo.dst[0] = W[0];
+    yo.g = g;
+    {
+      LaunchScope ls(c, KK_CONV_YINV);
+      if ((e2 = Launch<T>::conv_yinv(M, yo, M, Kz, 1, twM, s)) != cudaSuccess) return e2;
+    }
+    ZConvArgs<T> zc{};
+    zc.in[0] = W[0];
+    zc.out = R(dstf);
+    zc.nop = 1;
+    zc.kin = Kz;
+    zc.kout = H;
+    zc.in_stride = Kz;
+    zc.out_stride = H;
+    zc.nlines = M * M;
+    zc.out_scale = T(1);
+    zc.err = c->d_err;
+    LaunchScope ls(c, KK_CONV_Z);
+    return Launch<T>::z_c2r_tma(H, zc, twH, twM, s);
+  };
+
   // ---- phi(2) (ic_generator.cc:471-488) ----------------------------------
   // with 3LPT the convolve3 first stages (truncated pair products phi,00 phi,11
   // / phi,01 phi,02 / phi,12^2 / phi,02^2 / phi,01^2) come out of the same pass
   CK(hessians(0, 0));
-  mf_grid* qg[5] = {ic->tmp[0], ic->tmp[1], ic->tmp[2], ic->wn, ic->qx};
   CK(sources(p.lpt_order > 2 ? SRC_PHI2_PAIRS : SRC_PHI2));
   CK(r2c_unpad(P0, (cplx<T>*)ic->f[1]->d, OUT_ASSIGN, 1));
   ic->f[1]->space = MF_SPACE_K;
+  // the truncated pairs, from the slots of the phi(2) Hessians (still free)
+  // into their operand slots 12..16
   if (p.lpt_order > 2)
-    for (int k = 0; k < 5; ++k) CK(r2c_unpad(6 + k, (cplx<T>*)qg[k]->d, OUT_ASSIGN, 0));
+    for (int k = 0; k < 5; ++k) CK(truncate_pair(6 + k, 12 + k));
   if (timed) CK(cudaEventRecord(ic->ev[2], s));
   if (p.lpt_order > 2) {
     // ---- phi(3) (ic_generator.cc:511-528) --------------------------------
     CK(hessians(1, 6));
-    // the pairs' padded c2r
-    {
-      Operand<T> ops[3];
-      int dst[3];
-      for (int b0 = 0; b0 < 5; b0 += 3) {
-        const int nb = (5 - b0 < 3) ? 5 - b0 : 3;
-        for (int k = 0; k < nb; ++k) {
-          ops[k] = Operand<T>{};
-          ops[k].f = (const cplx<T>*)qg[b0 + k]->d;
-          ops[k].kind = OPND_PLAIN;
-          dst[k] = 12 + b0 + k;
-        }
-        CK(c2r(nb, ops, dst));
-      }
-    }
     CK(sources(SRC_PHI3_A3));
     CK(r2c_unpad(P0, (cplx<T>*)ic->f[2]->d, OUT_ASSIGN, 1));
     ic->f[2]->space = MF_SPACE_K;
@@ -1069,7 +1110,7 @@ extern "C" int mf_ic_device_footprint(const mf_ic_params* p, size_t* bytes) {
     const size_t M = (p->convolver == MF_CONV_ORSZAG) ? 3 * n / 2 : n;
     if (uses_shared_sources(p)) {
       const size_t nreal = (p->lpt_order > 2) ? 22 : 7;
-      conv = 3 * M * M * (n / 2 + 1) * 2 * ps + nreal * M * M * M * ps + (p->lpt_order > 2 ? grid : 0);
+      conv = 3 * M * M * (n / 2 + 1) * 2 * ps + nreal * M * M * M * ps;
     } else {
       const int nbuf = (p->convolver == MF_CONV_ORSZAG) ? 2 : 3;
       conv = (size_t)nbuf * M * M * (n / 2 + 1) * 2 * ps + (p->convolver == MF_CONV_ORSZAG ? grid : 0);
@@ -1109,7 +1150,6 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   cudaFree(ic->pltg);
   cudaFree(ic->stage);
   if (ic->conv) mf_conv_destroy(ic->conv);
-  if (ic->qx) mf_grid_destroy(ic->qx);
   cudaFree(ic->rf);
   cudaFree(ic->w3);
   cudaFree(ic->amp);
@@ -1239,7 +1279,6 @@ extern "C" int mf_ic_create(mf_ctx* c, const mf_ic_params* p, mf_ic** out) {
     cudaError_t e4 = cudaMalloc(&ic->rf, nreal * M * M * (M / 2) * cs);
     if (e4 == cudaSuccess) e4 = cudaMalloc(&ic->w3, 3 * M * M * (n / 2 + 1) * cs);
     if (e4 != cudaSuccess) return fail(cuda_err(c, e4, "mf_ic_create: shared-source buffers"));
-    if (p->lpt_order > 2 && (rc = mf_grid_create(c, n, p->boxlen, p->precision, MF_SPACE_K, &ic->qx))) return fail(rc);
   } else if (p->lpt_order > 1) {
     if ((rc = mf_conv_create(c, n, p->boxlen, p->precision, p->convolver, &ic->conv))) return fail(rc);
   }

@@ -70,6 +70,9 @@ struct Launch {
                                cudaStream_t s);
   static cudaError_t conv_xfwd(int L, ConvXFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                cudaStream_t s);
+  // convolve3's truncation of a pair product: x r2c pass, unpad, pad, x c2r pass
+  static cudaError_t conv_xtrunc(int L, ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                 cudaStream_t s);
   // z passes
   static cudaError_t z_r2c_plain(int H, PlainZOp<T> op, int nlines, int kout, const cplx<T>* twH,
                                  const cplx<T>* twM, cudaStream_t s);

@@ -190,6 +190,72 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 }
 
 // ---------------------------------------------------------------------------
+// strided forward transform, truncation and inverse transform of one column in
+// one pass (ConvXTruncOp), persistent and double-buffered as k_colfft_pipe
+// ---------------------------------------------------------------------------
+template <typename T, int L, int NCOL>
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
+                                  (NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL <= 256) ? 2 : 1)
+k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
+  using FF = LineFFT<T, L, false, MF_COL_MAXR>;
+  using FI = LineFFT<T, L, true, MF_COL_MAXR>;
+  static_assert(FF::E == FI::E && FF::TPL == FI::TPL, "one plan for both directions");
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + L * NCOL;
+  const int c = threadIdx.x, t = threadIdx.y;
+  const int total = ntc * nslab;
+  auto issue = [&](int tl, C* buf) {
+    const int ct = tl % ntc, slab = tl / ntc;
+    const int col = ct * NCOL + c;
+#pragma unroll
+    for (int s = 0; s < FF::E; ++s) {
+      const int e = FF::in_index(t, s);
+      C* d = buf + e * NCOL + c;
+      if (col < ncols) {
+        if constexpr (sizeof(C) == 16) cp_async16(d, op.at(slab, e, col)); else cp_async8(d, op.at(slab, e, col));
+      } else {
+        *d = mkc<T>(T(0), T(0));
+      }
+    }
+    cp_async_commit();
+  };
+  int tl = blockIdx.x;
+  if (tl < total) issue(tl, buf0); else cp_async_commit();
+  for (int it = 0; tl < total; tl += gridDim.x, ++it) {
+    C* cur = (it & 1) ? buf1 : buf0;
+    C* nxt = (it & 1) ? buf0 : buf1;
+    const int tn = tl + gridDim.x;
+    if (tn < total) issue(tn, nxt); else cp_async_commit();
+    cp_async_wait<1>();
+    const int ct = tl % ntc, slab = tl / ntc;
+    const int col = ct * NCOL + c;
+    const bool valid = col < ncols;
+    C v[FF::E];
+#pragma unroll
+    for (int s = 0; s < FF::E; ++s) v[s] = cur[FF::in_index(t, s) * NCOL + c];
+    FF::run(v, t, cur + c, NCOL, tw, SyncBlock{});
+    __syncthreads();  // the last exchange of the forward transform has been read
+#pragma unroll
+    for (int s = 0; s < FF::E; ++s) {
+      const int e = FF::out_index(t, s);
+      cur[e * NCOL + c] = op.mask(slab, e, col, v[s]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < FI::E; ++s) v[s] = cur[FI::in_index(t, s) * NCOL + c];
+    FI::run(v, t, cur + c, NCOL, tw, SyncBlock{});
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < FI::E; ++s) *op.at(slab, FI::out_index(t, s), col) = v[s];
+    }
+    __syncthreads();  // cur is refilled by the next iteration's copies
+  }
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // z pass, real -> half complex (forward), one line per thread group
 // OP: __device__ C load_pair(int line, int m) const;   // (x[2m], x[2m+1])
 //     __device__ void store(int line, int k, C v) const;  // k in [0, kout)

@@ -350,8 +350,37 @@ cudaError_t Launch<T>::conv_xfwd(int L, ConvXFwdOp<T> op, int nslab, int ncols, 
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
+template <typename T, int L>
+cudaError_t launch_xtrunc(ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T>* tw, cudaStream_t s) {
+  constexpr int NC = pipe_ncol<T, L>();
+  constexpr int TPL = LineFFT<T, L, false, MF_COL_MAXR>::TPL;
+  const size_t smem = (size_t)2 * L * NC * sizeof(cplx<T>);
+  auto kern = k_colfft_trunc<T, L, NC>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0, nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NC * TPL, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  const int ntc = (ncols + NC - 1) / NC;
+  const int total = ntc * nslab;
+  int grid = nsm * per_sm;
+  if (grid > total) grid = total;
+  kern<<<grid, dim3(NC, TPL), smem, s>>>(op, tw, ncols, ntc, nslab);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t Launch<T>::conv_xtrunc(int L, ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T>* tw,
+                                   cudaStream_t s) {
+#define CASE(LL) case LL: return launch_xtrunc<T, LL>(op, nslab, ncols, tw, s);
+  switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
+#undef CASE
+}
 template cudaError_t Launch<MF_T>::conv_xinv(int, ConvXInvOp<MF_T>, int, int, int, const cplx<MF_T>*, cudaStream_t);
 template cudaError_t Launch<MF_T>::conv_xfwd(int, ConvXFwdOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
+template cudaError_t Launch<MF_T>::conv_xtrunc(int, ConvXTruncOp<MF_T>, int, int, const cplx<MF_T>*, cudaStream_t);
 #endif
 
 #if defined(MF_PART_CONVY)

@@ -404,6 +404,27 @@ struct AssembleXInvOp {
   __device__ __forceinline__ void store(int j, int i, int kz, C v) const { dst[((long long)i * n + j) * Kz + kz] = v; }
 };
 
+// convolve3's intermediate truncation on a work buffer, in place: the x pass
+// of the pair product's r2c, the unpad to the N-cube with the Nyquist planes
+// zeroed (convolution.hh:618-653, op::assign_to), and the x pass of the
+// truncated field's padded c2r (pad_insert, convolution.hh:570-592) — the
+// unpadded N-grid never leaves the tile.  slab = j < N, e = x in [0, M), col = kz
+template <typename T>
+struct ConvXTruncOp {
+  using C = cplx<T>;
+  C* buf;  // work buffer, compact rows j < N of each x slab
+  ConvGeom g;
+  T scale_out, scale_in;  // the unpad factor of the r2c, the pad factor of the c2r
+  __device__ __forceinline__ C* at(int j, int x, int kz) const { return buf + ((long long)x * g.M + j) * g.Kz + kz; }
+  __device__ __forceinline__ C mask(int j, int x, int kz, C v) const {
+    const int i = g.kept_row(x);
+    const int nh = g.N >> 1;
+    if (i < 0 || (g.orszag && (i == nh || j == nh || kz == nh))) return mkc<T>(T(0), T(0));
+    v = mkc<T>(v.x * scale_out, v.y * scale_out);  // the unpadded value
+    return mkc<T>(v.x * scale_in, v.y * scale_in);  // the padded operand
+  }
+};
+
 // plain strided pass over an n-grid: element (slab, e, col) at
 // base[slab*slab_str + e*e_str + col]; in place, scale on store
 template <typename T>
