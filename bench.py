@@ -435,25 +435,13 @@ def run_mf(args):
     import numpy as np
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from monofonic_gb300 import replicas
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    job = replicas.init("nccl")  # replicas only: barrier and timing reductions, no data-path collective
+    world, rank, local = job.world, job.rank, job.local
+    barrier = job.barrier
+    max_over_ranks = job.max_over_ranks
 
     import monofonic_gb300 as mf
     from monofonic_gb300 import ic
@@ -656,8 +644,7 @@ def run_mf(args):
             "output": output,
         }
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    job.close()
     return 0
 
 

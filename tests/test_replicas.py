@@ -1,0 +1,63 @@
+"""Several GPUs of one node run replicas (monofonic_gb300/replicas.py): ranks
+meet only at a barrier and at reductions of their timings.  Two gloo ranks on
+the CPU exercise that host logic; the reference arm of bench.py prints on rank
+0 only."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    from monofonic_gb300 import replicas
+    job = replicas.init("gloo")
+    assert job.world == world and job.rank == rank and job.dist is not None
+    mx = job.max_over_ranks(1.5 + rank)
+    sm = job.sum_over_ranks(10.0 * (rank + 1))
+    # 100 units per rank, the slowest rank took 3 s: 200 / 3 units per second
+    rate = job.aggregate_rate(100.0, 2.0 + rank)
+    job.barrier()
+    job.close()
+    with open(os.path.join(out_dir, f"rank{rank}.txt"), "w") as f:
+        f.write(f"{mx} {sm} {rate}")
+
+
+def test_two_gloo_ranks(tmp_path):
+    import torch.multiprocessing as mp
+    port = _free_port()
+    mp.spawn(_rank_main, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    for r in range(2):
+        mx, sm, rate = map(float, (tmp_path / f"rank{r}.txt").read_text().split())
+        assert mx == 2.5 and sm == 30.0
+        assert rate == pytest.approx(200.0 / 3.0, rel=1e-15)
+
+
+def test_single_process_needs_no_group(monkeypatch):
+    from monofonic_gb300 import replicas
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    job = replicas.init("gloo")
+    assert job.world == 1 and job.dist is None and job.backend is None
+    assert job.max_over_ranks(4.0) == 4.0 and job.aggregate_rate(10.0, 2.0) == 5.0
+    job.barrier()
+    job.close()
+
+
+def test_reference_arm_prints_on_rank0_only():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1",
+                        "--warmup", "0"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert p.stdout.strip() == ""
