@@ -383,11 +383,12 @@ extern "C" int mf_ic_write_grafic2(mf_ic* ic, mf_grafic2* w) {
     return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: the pipeline must be created with out_kind = MF_OUT_FIELDS");
   if (p->ngrid != w->p.ngrid) return set_err(c, MF_ERR_SHAPE, "mf_ic_write_grafic2: setup/GridRes differs");
   // the plugin's units enter the fields (ic_generator.cc:815, :872-873)
-  if (p->lunit != w->p.boxlen || p->vunit != w->p.boxlen)
+  auto same = [](double a, double b) { return std::fabs(a - b) <= 1e-12 * std::fabs(b); };
+  if (!same(p->lunit, w->p.boxlen) || !same(p->vunit, w->p.boxlen))
     return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: pipeline units differ from the plugin's position/velocity unit");
   if (p->baryons && w->p.use_spt)
     return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: Lagrangian baryon fields (grafic_use_SPT) are not built");
-  if (p->baryons && p->munit != 1.0 / w->p.Omega_m)
+  if (p->baryons && !same(p->munit, 1.0 / w->p.Omega_m))
     return set_err(c, MF_ERR_ARG, "mf_ic_write_grafic2: pipeline mass unit differs from the plugin's (1 / Omega_m)");
   mf_particles dev[2] = {};
   dev[0].location = dev[1].location = MF_LOC_DEVICE;
