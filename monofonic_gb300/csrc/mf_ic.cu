@@ -17,11 +17,13 @@
 #include "mf_ppt.h"
 #include "mf_runtime.h"
 
-// host hand-off during a run (a build-time knob): 0 copies the positions
-// while the velocities are assembled; 1 streams the IDs and every
-// sub-lattice slice as soon as each is final
+// host hand-off during a run (a build-time knob).  The IDs are copied while
+// the run computes either way; 1 streams every sub-lattice slice of the
+// positions and velocities as soon as each is final (the copies queue on one
+// copy engine, so the tail after the last kernel is one slice); 0 copies the
+// positions during the velocity pass and the velocities after it
 #ifndef MF_STREAM_HANDOFF
-#define MF_STREAM_HANDOFF 0
+#define MF_STREAM_HANDOFF 1
 #endif
 
 namespace mf {
@@ -378,6 +380,7 @@ struct mf_ic {
   const mf_particles* early = nullptr;
   bool early_all = false;  // every particle array was streamed to the host during the run
   bool pos_early = false;  // the positions were copied during the run
+  bool ids_early = false;  // the IDs were copied during the run
   // shared-source convolutions: padded real fields and three work buffers
   bool shared = false;
   void* rf = nullptr;   // real padded fields [nreal][M*M][M/2] packed pairs (last 5 or 1: product sums)
@@ -725,7 +728,10 @@ int enqueue_impl(mf_ic* ic) {
     else
       k_ids<uint32_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint32_t*)ic->dids, n, overload, 0);
     CK(cudaGetLastError());
-    if (ic->early && MF_STREAM_HANDOFF) CK(early_copy(ic->early->ids, ic->dids, ic->id_bytes));
+    if (ic->early) {  // the IDs' copy overlaps the whole run
+      CK(early_copy(ic->early->ids, ic->dids, ic->id_bytes));
+      ic->ids_early = true;
+    }
     if (p.baryons) {  // baryon IDs start at IDoffset = 1 (ic_generator.cc:626-628)
       const uint64_t off = (uint64_t)overload * n * n * n;
       if (p.id64)
@@ -1069,7 +1075,7 @@ int handoff(mf_ic* ic, mf_particles* out) {
       if (!ic->early_all) {
         if (!ic->pos_early) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, s));
-        if (!fields) CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, s));
+        if (!fields && !ic->ids_early) CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, s));
       }
       if (ic->pos_early) CK(cudaStreamWaitEvent(s, ic->ev_copy, 0));  // the run ends after the streamed copies
     } else {
@@ -1446,6 +1452,7 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   ic->early = nullptr;
   ic->early_all = false;
   ic->pos_early = false;
+  ic->ids_early = false;
   if (out && out->location == MF_LOC_HOST && out->pos && out->vel &&
       (ic->p.out_kind == MF_OUT_FIELDS || out->ids)) {
     cudaError_t e = cudaSuccess;
@@ -1463,6 +1470,7 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   ic->early = nullptr;
   ic->early_all = false;
   ic->pos_early = false;
+  ic->ids_early = false;
   return rc;
 }
 
@@ -1515,6 +1523,7 @@ extern "C" int mf_ic_run_species(mf_ic* ic, mf_particles* out, int nspecies) {
   ic->early = nullptr;  // the hand-off happens after the run
   ic->early_all = false;
   ic->pos_early = false;
+  ic->ids_early = false;
   int rc = mf_ic_enqueue(ic);
   cudaError_t e = cudaSuccess;
   for (int sp = 0; sp < 2 && rc == MF_OK; ++sp) {
