@@ -178,3 +178,38 @@ def test_non_power_of_two_grid_bcc_f64(ctx):
     assert rel_l2(pos - q, rpos - q) < F64_TOL
     assert rel_l2(vel, rvel) < F64_TOL
     assert np.array_equal(ids, rids)
+
+
+def test_max_size_properties(ctx):
+    """the bench workload at its full size (3LPT + PLT, BCC 2x512^3, FP32-bulk):
+    size-independent properties where the oracle cannot follow — IDs exact
+    for every particle, every displacement and velocity finite, zero mean
+    displacement per sub-lattice and component (the DC mode is zeroed,
+    ic_generator.cc:858), velocities with zero mean likewise"""
+    from monofonic_gb300 import ic
+    n, L, z = 512, 1000.0, 24.0
+    cosmo, sc, osc = setup(z)
+    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=3, lattice="bcc", precision="f32", plt=True,
+                      lunit=L, vunit=L, pos64=False, id64=True)
+    g = ic.ICGenerator(ctx, cfg, sc)
+    g.set_noise_seed(20240)
+    pos, vel, ids = g.run()
+    n3 = n ** 3
+    assert ids.shape == (2 * n3,)
+    assert np.array_equal(ids[:n3], np.arange(n3, dtype=np.uint64) * 2)
+    assert np.array_equal(ids[n3:], np.arange(n3, dtype=np.uint64) * 2 + 1)
+    assert np.isfinite(pos).all() and np.isfinite(vel).all()
+    idx = np.arange(n, dtype=np.float64)
+    for ish, s in enumerate(O.LATTICE_SHIFTS[1]):
+        p = pos[ish * n3:(ish + 1) * n3].reshape(n, n, n, 3)
+        for d in range(3):
+            q = ((idx + s[d]) / n * L).astype(np.float64)
+            shape = [1, 1, 1]
+            shape[d] = n
+            disp = p[..., d].astype(np.float64) - q.reshape(shape)
+            rms = np.sqrt(np.mean(disp ** 2))
+            assert 0 < rms < 0.05 * L
+            assert abs(disp.mean()) < 1e-3 * rms, (ish, d)
+            v = vel[ish * n3:(ish + 1) * n3, d].astype(np.float64)
+            assert abs(v.mean()) < 1e-3 * np.sqrt(np.mean(v ** 2)), (ish, d)
+    g.close()
