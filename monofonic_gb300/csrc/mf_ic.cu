@@ -1082,6 +1082,7 @@ int handoff(mf_ic* ic, mf_particles* out) {
       out->pos = ic->dpos;
       out->vel = ic->dvel;
       out->ids = ic->dids;
+      out->mass = nullptr;  // single-species pipelines carry no per-particle masses
     }
   }
   CK(cudaEventRecord(ic->ev[8], s));
@@ -1481,6 +1482,7 @@ extern "C" int mf_ic_particles(mf_ic* ic, mf_particles* out) {
   out->ids = ic->dids;
   out->npart = ic->npart;
   out->location = MF_LOC_DEVICE;
+  out->mass = ic->dmass[0];  // dark-matter masses of a two-species pipeline, else null
   return MF_OK;
 }
 
