@@ -110,6 +110,15 @@ int mf_server_submit(mf_server* s, const mf_ic_request* req, int64_t* id);
 /* wait until request id has finished (timeout_s < 0: no limit);
  * MF_ERR_TIMEOUT if it has not finished in time */
 int mf_server_wait(mf_server* s, int64_t id, mf_request_result* out, double timeout_s);
+/* non-blocking status of request id: *done = 1 and *out filled (out may be
+ * NULL) once it has finished, else *done = 0 */
+int mf_server_poll(mf_server* s, int64_t id, mf_request_result* out, int* done);
+/* cancel request id.  A queued request is taken out of the queue and finishes
+ * at once with MF_ERR_CANCELLED.  A running request finishes with
+ * MF_ERR_CANCELLED at its next stage boundary (before its pipeline is
+ * enqueued, or between two output chunks); device work already enqueued
+ * completes.  MF_ERR_STATE if the request has already finished. */
+int mf_server_cancel(mf_server* s, int64_t id);
 /* wait until every submitted request has finished */
 int mf_server_drain(mf_server* s, double timeout_s);
 int mf_server_stats_get(mf_server* s, mf_server_stats* out);

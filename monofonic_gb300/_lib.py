@@ -174,6 +174,8 @@ SIGNATURES.update({
     "mf_server_create": (C.c_int, [C.c_int, C.POINTER(mf_server_config), C.POINTER(C.c_void_p)]),
     "mf_server_submit": (C.c_int, [C.c_void_p, C.POINTER(mf_ic_request), C.POINTER(C.c_int64)]),
     "mf_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(mf_request_result), C.c_double]),
+    "mf_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(mf_request_result), C.POINTER(C.c_int)]),
+    "mf_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
     "mf_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
     "mf_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(mf_server_stats)]),
     "mf_server_now": (C.c_double, [C.c_void_p]),

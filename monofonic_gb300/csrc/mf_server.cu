@@ -60,6 +60,7 @@ struct Req {
   mf_request_result res{};
   size_t need = 0;  // device footprint of a new pipeline for it
   bool done = false;
+  bool cancel = false;  // set by mf_server_cancel while the request runs
 };
 
 struct Staging {
@@ -149,6 +150,11 @@ struct mf_server {
     return false;
   }
 
+  bool cancelled(const Req* q) {
+    std::lock_guard<std::mutex> lk(mu);
+    return q->cancel;
+  }
+
   void finish(Req* q, int status) {
     std::lock_guard<std::mutex> lk(mu);
     q->res.status = status;
@@ -172,6 +178,7 @@ int mf_server::run_request(Req* q, Pipe* p, Staging& st) {
   if (rc != MF_OK) return rc;
   if ((rc = mf_ic_set_cosmology(p->ic, &sc)) != MF_OK) return rc;
   mf_ic_set_noise_seed(p->ic, q->r.seed);
+  if (cancelled(q)) return MF_ERR_CANCELLED;
   cudaStream_t s = p->ctx->stream;
   cudaEventRecord(p->g0, s);
   if ((rc = mf_ic_enqueue(p->ic)) != MF_OK) return rc;
@@ -218,6 +225,10 @@ int mf_server::run_request(Req* q, Pipe* p, Staging& st) {
   };
   if (issue(0) != cudaSuccess) return MF_ERR_CUDA;
   for (int64_t c = 0; c < nch; ++c) {
+    if (cancelled(q)) {  // let the copies in flight land before the buffers are reused
+      cudaStreamSynchronize(s);
+      return MF_ERR_CANCELLED;
+    }
     if (c + 1 < nch && issue(c + 1) != cudaSuccess) return MF_ERR_CUDA;
     if (cudaEventSynchronize(st.ev[c & 1]) != cudaSuccess) return MF_ERR_CUDA;
     const int64_t f = c * chunk, cnt = std::min<int64_t>(chunk, np - f);
@@ -364,6 +375,37 @@ extern "C" int mf_server_wait(mf_server* s, int64_t id, mf_request_result* out, 
   if (timeout_s < 0) s->cv_done.wait(lk, pred);
   else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return MF_ERR_TIMEOUT;
   if (out) *out = q->res;
+  return MF_OK;
+}
+
+extern "C" int mf_server_poll(mf_server* s, int64_t id, mf_request_result* out, int* done) {
+  if (!s || !done) return MF_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
+  const Req* q = s->reqs[id];
+  *done = q->done ? 1 : 0;
+  if (q->done && out) *out = q->res;
+  return MF_OK;
+}
+
+extern "C" int mf_server_cancel(mf_server* s, int64_t id) {
+  if (!s) return MF_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
+  Req* q = s->reqs[id];
+  if (q->done) return MF_ERR_STATE;
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+    if (*it == id) {  // never admitted: finishes now
+      s->queue.erase(it);
+      q->res.status = MF_ERR_CANCELLED;
+      q->res.t_done = s->now();
+      q->done = true;
+      ++s->failed;
+      s->cv_done.notify_all();
+      s->cv_work.notify_all();
+      return MF_OK;
+    }
+  q->cancel = true;  // running: stops at its next stage boundary
   return MF_OK;
 }
 

@@ -198,6 +198,22 @@ class Server:
             raise MFError(rc, "mf_server_wait")
         return {f: getattr(r, f) for f, _ in r._fields_}
 
+    def poll(self, rid: int) -> dict | None:
+        """the request's result if it has finished, else None (never blocks)"""
+        r = L.mf_request_result()
+        done = C.c_int()
+        rc = lib().mf_server_poll(self.ptr, int(rid), C.byref(r), C.byref(done))
+        if rc != L.MF_OK:
+            raise MFError(rc, "mf_server_poll")
+        return {f: getattr(r, f) for f, _ in r._fields_} if done.value else None
+
+    def cancel(self, rid: int):
+        """cancel a queued request (it never runs) or stop a running one at its
+        next stage boundary; MFError(MF_ERR_STATE) once it has finished"""
+        rc = lib().mf_server_cancel(self.ptr, int(rid))
+        if rc != L.MF_OK:
+            raise MFError(rc, "mf_server_cancel")
+
     def drain(self, timeout_s: float = -1.0):
         rc = lib().mf_server_drain(self.ptr, float(timeout_s))
         if rc != L.MF_OK:

@@ -180,6 +180,37 @@ def test_server_admission_respects_budget(ctx):
     srv.close()
 
 
+def test_server_poll_and_cancel(ctx):
+    """one worker: the first request is still creating its pipeline when the
+    last ones are cancelled, so they leave the queue without running; the
+    others finish normally and cancelling a finished request is an error"""
+    from monofonic_gb300 import _lib as L
+    from monofonic_gb300.serve import Server, Request
+    srv = Server(nworkers=1, output="count")
+    reqs = [Request(ngrid=128, boxlen=256.0, lpt_order=3, seed=1), Request(ngrid=32, boxlen=64.0, seed=2),
+            Request(ngrid=64, boxlen=128.0, seed=3), Request(ngrid=64, boxlen=128.0, seed=4)]
+    ids = [srv.submit(r) for r in reqs]
+    srv.cancel(ids[2])
+    srv.cancel(ids[3])
+    for i in (2, 3):  # finished at once, never admitted
+        res = srv.poll(ids[i])
+        assert res is not None and res["status"] == L.MF_ERR_CANCELLED and res["t_admit"] == 0.0
+    srv.drain(300.0)
+    for i in (0, 1):
+        res = srv.poll(ids[i])
+        assert res is not None and res["status"] == 0 and res["npart"] == reqs[i].npart
+        assert res == srv.wait(ids[i])
+    st = srv.stats()
+    assert st["completed"] == 2 and st["failed"] == 2 and st["queued"] == 0
+    assert srv.bytes_out == sum(r.npart * 56 for r in reqs[:2])  # FP64 positions and velocities, u64 IDs
+    with pytest.raises(L.MFError) as e:
+        srv.cancel(ids[0])
+    assert e.value.code == L.MF_ERR_STATE
+    with pytest.raises(L.MFError):
+        srv.poll(len(ids))
+    srv.close()
+
+
 def test_autotune_keeps_parity(ctx):
     """the autotuner changes schedules only: a convolution after tuning still
     matches the oracle (FP64 1e-12), and the report names every pass"""
