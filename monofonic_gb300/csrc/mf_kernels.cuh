@@ -22,6 +22,13 @@
 #ifndef MF_COL_MAXR
 #define MF_COL_MAXR 8
 #endif
+// threads per CTA up to which the pipelined strided passes are compiled for two
+// resident CTAs per SM (a register cap of 65536 / (2 x threads)); a build-time knob.
+// 512 puts two 512-thread CTAs of the FP32 length-512 passes on an SM (64
+// registers, no spills): 0.4 ms less per 512^3 3LPT IC than one CTA at 256.
+#ifndef MF_COL_MINB_LIMIT
+#define MF_COL_MINB_LIMIT 512
+#endif
 
 namespace mf {
 
@@ -117,7 +124,7 @@ k_colfft3(OP op, const cplx<T>* __restrict__ tw, int ncols) {
 // ---------------------------------------------------------------------------
 template <typename T, int L, bool INV, int NCOL, class OP>
 __global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
-                                  (NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL <= 256) ? 2 : 1)
+                                  (NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL <= MF_COL_MINB_LIMIT) ? 2 : 1)
 k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
   using F = LineFFT<T, L, INV, MF_COL_MAXR>;
   using C = cplx<T>;
@@ -195,7 +202,7 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 // ---------------------------------------------------------------------------
 template <typename T, int L, int NCOL>
 __global__ void __launch_bounds__(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
-                                  (NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL <= 256) ? 2 : 1)
+                                  (NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL <= MF_COL_MINB_LIMIT) ? 2 : 1)
 k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
   using FF = LineFFT<T, L, false, MF_COL_MAXR>;
   using FI = LineFFT<T, L, true, MF_COL_MAXR>;
