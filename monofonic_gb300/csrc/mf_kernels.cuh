@@ -29,8 +29,29 @@
 #ifndef MF_COL_MINB_LIMIT
 #define MF_COL_MINB_LIMIT 512
 #endif
+// 1: the pipelined strided passes' resident CTAs per SM sized from the
+// registers the plan needs (~4 per scalar held, plus 32) instead of the rule
+// above, at most 4; a build-time knob.  The 128-thread CTAs of the FP32
+// length-96..384 passes were compiled for two CTAs per SM and took up to 255
+// registers (8 warps per SM); sized for four (128 registers, no spills) the
+// N=256 3LPT IC takes 10.9 instead of 11.7 ms and the 96-realization batch
+// 215 instead of 231 ms.  M=768 and N=512 passes compile as before.
+#ifndef MF_COL_REG_SIZED
+#define MF_COL_REG_SIZED 1
+#endif
 
 namespace mf {
+
+// minimum resident CTAs per SM a pipelined strided pass is compiled for
+// (its __launch_bounds__): threads per CTA, values per thread E of the plan,
+// bytes per scalar
+__host__ __device__ constexpr int col_minb(int threads, int e, int scalar_bytes) {
+  if (!MF_COL_REG_SIZED) return threads <= MF_COL_MINB_LIMIT ? 2 : 1;
+  int need = 4 * e * (scalar_bytes / 4) + 32;
+  need = need < 64 ? 64 : (need > 255 ? 255 : need);
+  const int b = 65536 / (threads * need);
+  return b < 1 ? 1 : (b > 4 ? 4 : b);
+}
 
 // ops with a per-tile prologue (tile_prep / xform_tile) in the pipelined pass
 template <class OP, class = void>
@@ -124,7 +145,8 @@ k_colfft3(OP op, const cplx<T>* __restrict__ tw, int ncols) {
 // ---------------------------------------------------------------------------
 template <typename T, int L, bool INV, int NCOL, class OP>
 __global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
-                                  (NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL <= MF_COL_MINB_LIMIT) ? 2 : 1)
+                                  col_minb(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
+                                           LineFFT<T, L, INV, MF_COL_MAXR>::E, (int)sizeof(T)))
 k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
   using F = LineFFT<T, L, INV, MF_COL_MAXR>;
   using C = cplx<T>;
@@ -202,7 +224,8 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 // ---------------------------------------------------------------------------
 template <typename T, int L, int NCOL>
 __global__ void __launch_bounds__(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
-                                  (NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL <= MF_COL_MINB_LIMIT) ? 2 : 1)
+                                  col_minb(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
+                                           LineFFT<T, L, false, MF_COL_MAXR>::E, (int)sizeof(T)))
 k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
   using FF = LineFFT<T, L, false, MF_COL_MAXR>;
   using FI = LineFFT<T, L, true, MF_COL_MAXR>;
