@@ -108,10 +108,14 @@ int mf_server_create(int device, const mf_server_config* cfg, mf_server** out);
 /* enqueue a request; returns its id in *id (ids start at 0) */
 int mf_server_submit(mf_server* s, const mf_ic_request* req, int64_t* id);
 /* wait until request id has finished (timeout_s < 0: no limit);
- * MF_ERR_TIMEOUT if it has not finished in time */
+ * MF_ERR_TIMEOUT if it has not finished in time, MF_ERR_STATE once released */
 int mf_server_wait(mf_server* s, int64_t id, mf_request_result* out, double timeout_s);
+/* free the record of a finished request (a long-running server otherwise
+ * keeps one per request until mf_server_destroy); its id then answers
+ * MF_ERR_STATE.  MF_ERR_STATE if it has not finished or was released */
+int mf_server_release(mf_server* s, int64_t id);
 /* non-blocking status of request id: *done = 1 and *out filled (out may be
- * NULL) once it has finished, else *done = 0 */
+ * NULL) once it has finished, else *done = 0; MF_ERR_STATE once released */
 int mf_server_poll(mf_server* s, int64_t id, mf_request_result* out, int* done);
 /* cancel request id.  A queued request is taken out of the queue and finishes
  * at once with MF_ERR_CANCELLED.  A running request finishes with

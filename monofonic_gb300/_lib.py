@@ -176,6 +176,7 @@ SIGNATURES.update({
     "mf_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(mf_request_result), C.c_double]),
     "mf_server_poll": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(mf_request_result), C.POINTER(C.c_int)]),
     "mf_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
+    "mf_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "mf_server_drain": (C.c_int, [C.c_void_p, C.c_double]),
     "mf_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(mf_server_stats)]),
     "mf_server_now": (C.c_double, [C.c_void_p]),

@@ -370,11 +370,25 @@ extern "C" int mf_server_wait(mf_server* s, int64_t id, mf_request_result* out, 
   if (!s) return MF_ERR_ARG;
   std::unique_lock<std::mutex> lk(s->mu);
   if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
-  Req* q = s->reqs[id];
-  auto pred = [&] { return q->done; };
+  // looked up again after every wake-up: another thread may release the record
+  auto pred = [&] { return !s->reqs[id] || s->reqs[id]->done; };
   if (timeout_s < 0) s->cv_done.wait(lk, pred);
   else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return MF_ERR_TIMEOUT;
+  const Req* q = s->reqs[id];
+  if (!q) return MF_ERR_STATE;
   if (out) *out = q->res;
+  return MF_OK;
+}
+
+extern "C" int mf_server_release(mf_server* s, int64_t id) {
+  if (!s) return MF_ERR_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
+  Req* q = s->reqs[id];
+  if (!q || !q->done) return MF_ERR_STATE;
+  delete q;
+  s->reqs[id] = nullptr;
+  s->cv_done.notify_all();  // waiters on this id return MF_ERR_STATE
   return MF_OK;
 }
 
@@ -383,6 +397,7 @@ extern "C" int mf_server_poll(mf_server* s, int64_t id, mf_request_result* out, 
   std::lock_guard<std::mutex> lk(s->mu);
   if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
   const Req* q = s->reqs[id];
+  if (!q) return MF_ERR_STATE;
   *done = q->done ? 1 : 0;
   if (q->done && out) *out = q->res;
   return MF_OK;
@@ -393,7 +408,7 @@ extern "C" int mf_server_cancel(mf_server* s, int64_t id) {
   std::lock_guard<std::mutex> lk(s->mu);
   if (id < 0 || id >= (int64_t)s->reqs.size()) return MF_ERR_ARG;
   Req* q = s->reqs[id];
-  if (q->done) return MF_ERR_STATE;
+  if (!q || q->done) return MF_ERR_STATE;
   for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
     if (*it == id) {  // never admitted: finishes now
       s->queue.erase(it);

@@ -214,6 +214,16 @@ class Server:
         if rc != L.MF_OK:
             raise MFError(rc, "mf_server_cancel")
 
+    def release(self, rid: int):
+        """free a finished request's record here and in the server (its
+        collected particles are dropped); its id is then unknown"""
+        rc = lib().mf_server_release(self.ptr, int(rid))
+        if rc != L.MF_OK:
+            raise MFError(rc, "mf_server_release")
+        with self._lock:
+            self._reqs.pop(rid, None)
+            self.results.pop(rid, None)
+
     def drain(self, timeout_s: float = -1.0):
         rc = lib().mf_server_drain(self.ptr, float(timeout_s))
         if rc != L.MF_OK:

@@ -208,6 +208,15 @@ def test_server_poll_and_cancel(ctx):
     assert e.value.code == L.MF_ERR_STATE
     with pytest.raises(L.MFError):
         srv.poll(len(ids))
+    # released records answer MF_ERR_STATE; the others stay readable
+    srv.release(ids[0])
+    srv.release(ids[2])
+    for call in (srv.poll, srv.wait, srv.release, srv.cancel):
+        with pytest.raises(L.MFError) as e:
+            call(ids[0])
+        assert e.value.code == L.MF_ERR_STATE
+    assert srv.poll(ids[1])["status"] == 0 and srv.stats()["completed"] == 2
+    srv.drain(10.0)
     srv.close()
 
 
