@@ -19,7 +19,8 @@ import numpy as np
 from . import _lib as L
 from ._lib import MFError
 
-__all__ = ["Context", "Grid_FFT", "OrszagConvolver", "NaiveConvolver", "op", "MFError", "lib"]
+__all__ = ["Context", "Grid_FFT", "OrszagConvolver", "NaiveConvolver", "op", "MFError", "lib", "grid_sizes",
+           "grid_wave_vector", "grid_gradient", "grid_laplacian"]
 
 
 def lib():
@@ -91,6 +92,37 @@ class Context:
             pass
 
 
+def grid_sizes(n: int, space: str):
+    """Grid_FFT::size(0..3) (src/grid_fft.cc:100-110, single process): the
+    three extents and the stored row length, (n, n, n, n+2) in real space and
+    (n, n, n/2+1, n/2+1) in k-space"""
+    return (n, n, n, n + 2) if space == "r" else (n, n, n // 2 + 1, n // 2 + 1)
+
+
+def grid_wave_vector(n: int, boxlen: float, i: int, j: int, k: int, dtype=np.float64) -> np.ndarray:
+    """Grid_FFT::get_k (include/grid_fft.hh:281-296, single process): per axis
+    (idx - n*[idx > n/2]) * 2pi/L in the grid's real type, the Nyquist index
+    staying positive"""
+    kfac = dtype(2.0 * np.pi / boxlen)
+    half = n // 2
+    return np.array([(dtype(x) - dtype(x > half) * dtype(n)) * kfac for x in (i, j, k)], dtype=dtype)
+
+
+def grid_gradient(n: int, boxlen: float, idim: int, ijk, dtype=np.float64) -> complex:
+    """Grid_FFT::gradient (include/grid_fft.hh:376-385): i k_idim, zero at the
+    Nyquist index of that axis"""
+    x = int(ijk[idim])
+    if x == n // 2:
+        return complex(0.0, 0.0)
+    return complex(0.0, float(grid_wave_vector(n, boxlen, *ijk, dtype=dtype)[idim]))
+
+
+def grid_laplacian(n: int, boxlen: float, ijk, dtype=np.float64) -> float:
+    """Grid_FFT::laplacian (include/grid_fft.hh:387-390): -|k|^2"""
+    kv = grid_wave_vector(n, boxlen, *ijk, dtype=dtype)
+    return float(-(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]))
+
+
 class Grid_FFT:
     """Device-resident Grid_FFT<real_t>: n^3 real grid in the padded in-place
     layout (n+2)*n*n reals, k-space (n, n, n/2+1) complex in place."""
@@ -148,8 +180,34 @@ class Grid_FFT:
     def get_real(self) -> np.ndarray:
         return self.download_padded()[:, :, : self.n].copy()
 
-    def get_k(self) -> np.ndarray:
+    def get_k(self, i=None, j=None, k=None) -> np.ndarray:
+        """with indices: the wave vector of mode (i, j, k), Grid_FFT::get_k
+        (include/grid_fft.hh:281-296); without: the k-space field as an
+        (n, n, n/2+1) complex host array"""
+        if i is not None:
+            return grid_wave_vector(self.n, self.L, i, j, k, self.dtype)
         return self.download_padded().view(self.cdtype).reshape(self.n, self.n, self.n // 2 + 1).copy()
+
+    # -- index helpers (host arithmetic, include/grid_fft.hh:121-390) -------
+    def size(self, i: int) -> int:
+        return grid_sizes(self.n, self.space)[i]
+
+    def get_idx(self, i: int, j: int, k: int) -> int:
+        """linear index of element (i, j, k) in the stored layout"""
+        sz = grid_sizes(self.n, self.space)
+        return (i * sz[1] + j) * sz[3] + k
+
+    def get_dx(self, idim: int = 0) -> float:
+        return float(self.dtype(self.L / self.n))
+
+    def get_k3(self, i: int, j: int, k: int):
+        return (i, j, k)
+
+    def gradient(self, idim: int, ijk) -> complex:
+        return grid_gradient(self.n, self.L, idim, ijk, self.dtype)
+
+    def laplacian(self, ijk) -> float:
+        return grid_laplacian(self.n, self.L, ijk, self.dtype)
 
     # -- Grid_FFT methods ---------------------------------------------------
     def fill_white_noise(self, seed: int):

@@ -91,3 +91,27 @@ def test_invalid_parameters_are_refused(scalars, change, code):
     with pytest.raises(L.MFError) as e:
         ic.device_footprint(cfg, scalars)
     assert e.value.code == code
+
+
+def test_grid_index_and_wave_vector_helpers():
+    """Grid_FFT::size / get_idx / get_k / gradient / laplacian of the Python
+    mirror (host arithmetic) against the oracle's per-axis k and gradient"""
+    import numpy as np
+    import monofonic_gb300 as mf
+    from oracle import lpt_oracle as O
+    n, L = 16, 100.0
+    assert mf.grid_sizes(n, "r") == (16, 16, 16, 18) and mf.grid_sizes(n, "k") == (16, 16, 9, 9)
+    k1, g1 = O.kvec_1d(n, L), O.grad_1d(n, L)
+    for i in range(n):
+        for j in range(0, n, 3):
+            for k in range(n // 2 + 1):
+                kv = mf.grid_wave_vector(n, L, i, j, k)
+                assert np.array_equal(kv, [k1[i], k1[j], k1[k]])
+                for d, x in enumerate((i, j, k)):
+                    assert mf.grid_gradient(n, L, d, (i, j, k)) == complex(0.0, g1[x])
+                assert mf.grid_laplacian(n, L, (i, j, k)) == -(k1[i] ** 2 + k1[j] ** 2 + k1[k] ** 2)
+    # FP32 grids compute in float: the same formula in single precision
+    kv32 = mf.grid_wave_vector(n, L, 9, 3, 8, np.float32)
+    kf = np.float32(2.0 * np.pi / L)
+    assert kv32.dtype == np.float32
+    assert np.array_equal(kv32, [np.float32(-7) * kf, np.float32(3) * kf, np.float32(8) * kf])
