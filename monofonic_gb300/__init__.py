@@ -188,6 +188,39 @@ class Grid_FFT:
             return grid_wave_vector(self.n, self.L, i, j, k, self.dtype)
         return self.download_padded().view(self.cdtype).reshape(self.n, self.n, self.n // 2 + 1).copy()
 
+    # -- element reads (include/grid_fft.hh:179-211) ------------------------
+    def _read(self, idx: int, count: int, dtype) -> np.ndarray:
+        if not 0 <= idx < count:
+            raise IndexError(f"element {idx} outside the grid's {count} stored elements")
+        self.ctx.synchronize()  # the grid's kernels run on the context's stream
+        out = np.empty(1, dtype=dtype)
+        rc = lib().mf_copy_to_host(out.ctypes.data, C.c_void_p(self.device_ptr() + idx * out.itemsize),
+                                   out.itemsize)
+        if rc != L.MF_OK:
+            raise MFError(rc, "mf_copy_to_host")
+        return out
+
+    def relem(self, i: int, j: int = None, k: int = None):
+        """relem(i, j, k) or relem(idx): one real element of the stored
+        (n, n, n+2) layout, read from the device"""
+        idx = i if j is None else (i * self.n + j) * (self.n + 2) + k
+        return self._read(idx, (self.n + 2) * self.n * self.n, self.dtype)[0]
+
+    def kelem(self, i: int, j: int = None, k: int = None):
+        """kelem(i, j, k) or kelem(idx): one complex mode of the stored
+        (n, n, n/2+1) layout, read from the device"""
+        idx = i if j is None else (i * self.n + j) * (self.n // 2 + 1) + k
+        return self._read(idx, self.n * self.n * (self.n // 2 + 1), self.cdtype)[0]
+
+    def get_r(self, i: int, j: int, k: int) -> np.ndarray:
+        """Grid_FFT::get_r (include/grid_fft.hh:218-228): cell position (i, j, k) * dx"""
+        dx = self.dtype(self.L / self.n)
+        return np.array([self.dtype(i) * dx, self.dtype(j) * dx, self.dtype(k) * dx], dtype=self.dtype)
+
+    def reset(self):
+        """Grid_FFT::reset: free the device memory (the object is unusable after)"""
+        self.close()
+
     # -- index helpers (host arithmetic, include/grid_fft.hh:121-390) -------
     def size(self, i: int) -> int:
         return grid_sizes(self.n, self.space)[i]

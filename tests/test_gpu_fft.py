@@ -31,6 +31,28 @@ def test_r2c_c2r(ctx, n, prec):
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_element_reads(ctx, prec):
+    """relem / kelem (grid_fft.hh:179-211) by (i, j, k) and by get_idx read the
+    stored layouts element for element"""
+    import monofonic_gb300 as mf
+    n = 16
+    x = np.random.default_rng(3).standard_normal((n, n, n))
+    g = mf.Grid_FFT(ctx, n, 100.0, prec)
+    g.set_real(x)
+    assert g.space == "r" and g.size(3) == n + 2
+    assert g.relem(2, 3, 4) == g.get_real()[2, 3, 4]
+    assert g.relem(g.get_idx(5, 6, 7)) == x.astype(g.dtype)[5, 6, 7]
+    g.FourierTransformForward()
+    X = g.get_k()
+    assert g.space == "k" and g.size(3) == n // 2 + 1
+    assert g.kelem(1, 2, 3) == X[1, 2, 3]
+    assert g.kelem(g.get_idx(4, 0, 8)) == X[4, 0, 8]
+    with pytest.raises(IndexError):
+        g.kelem(n, 0, 0)
+    g.close()
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
 @pytest.mark.parametrize("n", [16, 48 * 2, 128])
 def test_c2r_non_hermitian(ctx, n, prec):
     """c2r of a spectrum that is not Hermitian on the kz=0 and kz=n/2 planes:
