@@ -2,8 +2,8 @@
  *
  * Replaces src/plugins/output_grafic2.cc (class grafic2_output_plugin, registered
  * as "grafic2"), the one output format of the reference that needs no external
- * library (the HDF5 and GenericIO formats need libraries this build does not
- * carry).  The writer takes a real-space field on the device, transposes it to
+ * library (the HDF5 and GenericIO formats need the HDF5 and GenericIO
+ * libraries, which this library does not link).  The writer takes a real-space field on the device, transposes it to
  * the file's plane order and converts it to float on the GPU, and streams the
  * planes through two page-locked staging buffers, so the copy of one chunk of
  * planes overlaps the file write of the previous one.
