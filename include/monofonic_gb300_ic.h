@@ -40,7 +40,10 @@ typedef struct {
   double n_s, h, H0, Omega_m, Omega_b, Omega_r, Omega_DE, Tcmb;
 } mf_cosmo_scalars;
 
-/* fill *p with the documented defaults for unset keys */
+/* fill every field of *p with the Planck2018EE+BAO+SN set
+ * (src/cosmology_parameters.cc:89), the values ParameterSet = none gives the
+ * keys a configuration leaves unset (include/cosmology_parameters.hh:84-150);
+ * call it first, then set the keys the configuration holds */
 void mf_cosmo_params_default(mf_cosmo_params* p);
 /* cosmology::calculator ctor + scalars at z_start */
 int mf_cosmology_compute(const mf_cosmo_params* p, double zstart, mf_cosmo_scalars* out);
