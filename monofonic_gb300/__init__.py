@@ -185,6 +185,8 @@ class Grid_FFT:
         (include/grid_fft.hh:281-296); without: the k-space field as an
         (n, n, n/2+1) complex host array"""
         if i is not None:
+            if j is None or k is None:
+                raise TypeError("get_k takes three mode indices (i, j, k) or none")
             return grid_wave_vector(self.n, self.L, i, j, k, self.dtype)
         return self.download_padded().view(self.cdtype).reshape(self.n, self.n, self.n // 2 + 1).copy()
 
