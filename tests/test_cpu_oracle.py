@@ -118,3 +118,21 @@ def test_host_noise_golden_fixture(mflib):
     for nt in (1, 4):
         assert np.array_equal(ic.white_noise(16, 12345, nthreads=nt), ref)
     assert np.allclose(ref, O.white_noise(16, 12345), rtol=1e-14, atol=1e-14)
+
+
+def test_oracle_reproduces_the_lpt_fixture(mflib):
+    """the committed 3LPT BCC particles (tests/golden/make_lpt_fixture.py) are
+    what the oracle computes today: a change to the oracle shows up here"""
+    from monofonic_gb300 import ic
+    from tests.ic_helpers import setup
+    g = np.load(os.path.join(ROOT, "tests", "golden", "lpt3_bcc_n16_seed777.npz"))
+    n, L, z, order, lat = int(g["n"]), float(g["boxlen"]), float(g["zstart"]), int(g["order"]), int(g["lattice"])
+    _, sc, osc = setup(z)
+    assert math.isclose(sc.Dplus, float(g["Dplus"]), rel_tol=1e-14)
+    f = O.lpt_potentials(ic.white_noise(n, int(g["seed"])), L, order, osc)
+    pos, vel, ids = O.particles(f, L, order, osc.vfac, lattice=lat, lunit=L, vunit=L)
+    assert np.array_equal(ids, g["ids"])
+    from tests.ic_helpers import lattice_q
+    q = lattice_q(n, lat, L)  # compare displacements: positions minus the lattice
+    assert np.linalg.norm((pos - q) - (g["pos"] - q)) / np.linalg.norm(g["pos"] - q) < 1e-13
+    assert np.linalg.norm(vel - g["vel"]) / np.linalg.norm(g["vel"]) < 1e-13
