@@ -223,6 +223,70 @@ class Grid_FFT:
         """Grid_FFT::reset: free the device memory (the object is unusable after)"""
         self.close()
 
+    # -- functions of the field on the host mirror (grid_fft.hh:450-810) ----
+    # The reference loops a functor over every element on the CPU.  Here the
+    # field is read back, f is applied to whole numpy arrays (broadcasting
+    # replaces the element loop) and the result is written back, in the
+    # space the grid is in.  The pipeline's own k-space operators run as
+    # CUDA kernels; these are for arbitrary user functions.
+    def _k_arrays(self):
+        n = self.n
+        kfac = self.dtype(2.0 * np.pi / self.L)
+        idx = np.arange(n)
+        k1 = ((idx.astype(self.dtype) - (idx > n // 2).astype(self.dtype) * self.dtype(n)) * kfac).astype(self.dtype)
+        return k1[:, None, None], k1[None, :, None], k1[None, None, : n // 2 + 1]
+
+    def _r_arrays(self):
+        dx = self.dtype(self.L / self.n)
+        r1 = (np.arange(self.n).astype(self.dtype) * dx).astype(self.dtype)
+        return r1[:, None, None], r1[None, :, None], r1[None, None, :]
+
+    def _put_k(self, X):
+        a = np.ascontiguousarray(np.broadcast_to(X, (self.n, self.n, self.n // 2 + 1)), dtype=self.cdtype)
+        self.upload_padded(a.view(self.dtype).reshape(self.n, self.n, self.n + 2), self.space)
+
+    def _put_r(self, x):
+        a = self.download_padded()
+        a[:, :, : self.n] = x
+        self.upload_padded(a, self.space)
+
+    def apply_function_k(self, f):
+        """kelem <- f(kelem) (grid_fft.hh:450-465)"""
+        self._put_k(f(self.get_k()))
+
+    def apply_function_r(self, f):
+        """relem <- f(relem) (grid_fft.hh:467-482)"""
+        self._put_r(f(self.get_real()))
+
+    def apply_function_k_dep(self, f):
+        """kelem <- f(kelem, k) with k = (kx, ky, kz) broadcastable arrays
+        (grid_fft.hh:776-791)"""
+        self._put_k(f(self.get_k(), self._k_arrays()))
+
+    def apply_function_r_dep(self, f):
+        """relem <- f(relem, r) with r = (x, y, z) cell positions
+        (grid_fft.hh:793-808)"""
+        self._put_r(f(self.get_real(), self._r_arrays()))
+
+    def assign_function_of_grids_r(self, f, *grids):
+        """relem <- f(g1.relem, g2.relem, ...) (grid_fft.hh:697-714)"""
+        self._put_r(f(*[g.get_real() for g in grids]))
+
+    def assign_function_of_grids_k(self, f, *grids):
+        """kelem <- f(g1.kelem, g2.kelem, ...) (grid_fft.hh:716-734)"""
+        self._put_k(f(*[g.get_k() for g in grids]))
+
+    def assign_function_of_grids_ijk(self, f, *grids):
+        """kelem <- f((i, j, k), g1.kelem, ...) with broadcastable index arrays
+        (grid_fft.hh:736-754)"""
+        n = self.n
+        ijk = (np.arange(n)[:, None, None], np.arange(n)[None, :, None], np.arange(n // 2 + 1)[None, None, :])
+        self._put_k(f(ijk, *[g.get_k() for g in grids]))
+
+    def assign_function_of_grids_kdep(self, f, *grids):
+        """kelem <- f(k, g1.kelem, ...) (grid_fft.hh:756-774)"""
+        self._put_k(f(self._k_arrays(), *[g.get_k() for g in grids]))
+
     # -- index helpers (host arithmetic, include/grid_fft.hh:121-390) -------
     def size(self, i: int) -> int:
         return grid_sizes(self.n, self.space)[i]
