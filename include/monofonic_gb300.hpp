@@ -27,12 +27,15 @@
 #define MONOFONIC_GB300_HPP
 
 #include <array>
+#include <cmath>
 #include <complex>
 #include <cstddef>
 #include <cstdint>
+#include <initializer_list>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "monofonic_gb300.h"
@@ -92,6 +95,18 @@ inline context& default_context() {
 
 /* include/grid_fft.hh:29 */
 enum space_t { kspace_id, rspace_id };
+
+/* the 3-vector the reference's functors receive (include/math/vec3.hh:23-110:
+ * x, y, z, operator[], dot, norm_squared, norm) */
+template <typename T>
+struct vec3 {
+  T x{}, y{}, z{};
+  T& operator[](size_t i) noexcept { return i == 0 ? x : (i == 1 ? y : z); }
+  const T& operator[](size_t i) const noexcept { return i == 0 ? x : (i == 1 ? y : z); }
+  T dot(const vec3& a) const noexcept { return x * a.x + y * a.y + z * a.z; }
+  T norm_squared() const noexcept { return dot(*this); }
+  T norm() const noexcept { return std::sqrt(norm_squared()); }
+};
 
 /* Grid_FFT<real_t>: an n^3 field in HBM in the reference's in-place padded
  * layout, (n+2) reals per row in real space, n/2+1 complex per row in
@@ -157,11 +172,20 @@ class Grid_FFT {
   real_t get_dx(int idim) const { return length_[idim] / static_cast<real_t>(n_[idim]); }
   std::array<size_t, 3> get_k3(size_t i, size_t j, size_t k) const { return {i, j, k}; }
 
+  /* grid_fft.hh:218-228 */
+  template <typename ft>
+  vec3<ft> get_r(size_t i, size_t j, size_t k) const {
+    vec3<ft> r;
+    r.x = static_cast<ft>(static_cast<real_t>(i) * get_dx(0));
+    r.y = static_cast<ft>(static_cast<real_t>(j) * get_dx(1));
+    r.z = static_cast<ft>(static_cast<real_t>(k) * get_dx(2));
+    return r;
+  }
   /* grid_fft.hh:281-296: (idx - n [idx > n/2]) 2pi/L per axis */
   template <typename ft>
-  std::array<ft, 3> get_k(size_t i, size_t j, size_t k) const {
+  vec3<ft> get_k(size_t i, size_t j, size_t k) const {
     const size_t idx[3] = {i, j, k};
-    std::array<ft, 3> kk;
+    vec3<ft> kk;
     for (int d = 0; d < 3; ++d) {
       const real_t kfac = static_cast<real_t>(detail::two_pi / length_[d]);
       kk[d] = static_cast<ft>((static_cast<real_t>(idx[d]) -
@@ -242,6 +266,60 @@ class Grid_FFT {
     detail::check(ctx_->get(), mf_grid_fill_real64(handle(), x.data()), "mf_grid_fill_real64");
   }
 
+  /* functions of the field on the host mirror (grid_fft.hh:450-810): the
+   * field is read back, the functor runs per element on the host as in the
+   * reference, and the result is written back in the grid's current space.
+   * The pipeline's own k-space operators are CUDA kernels; these serve
+   * arbitrary user functors. */
+  template <typename F>
+  void apply_function_k(const F& f) {
+    each_k([&](size_t, size_t, size_t, size_t c, std::vector<real_t>& out) { put_c(out, c, f(get_c(out, c))); });
+  }
+  template <typename F>
+  void apply_function_r(const F& f) {
+    each_r([&](size_t, size_t, size_t, size_t r, std::vector<real_t>& out) { out[r] = f(out[r]); });
+  }
+  template <typename F>
+  void apply_function_k_dep(const F& f) {
+    each_k([&](size_t i, size_t j, size_t k, size_t c, std::vector<real_t>& out) {
+      put_c(out, c, f(get_c(out, c), get_k<real_t>(i, j, k)));
+    });
+  }
+  template <typename F>
+  void apply_function_r_dep(const F& f) {
+    each_r([&](size_t i, size_t j, size_t k, size_t r, std::vector<real_t>& out) {
+      out[r] = f(out[r], get_r<real_t>(i, j, k));
+    });
+  }
+  template <typename F, typename... G>
+  void assign_function_of_grids_r(const F& f, G&... grids) {
+    const auto in = read_all(grids...);
+    each_r([&](size_t, size_t, size_t, size_t r, std::vector<real_t>& out) {
+      out[r] = call_r(f, in, r, std::index_sequence_for<G...>{});
+    });
+  }
+  template <typename F, typename... G>
+  void assign_function_of_grids_k(const F& f, G&... grids) {
+    const auto in = read_all(grids...);
+    each_k([&](size_t, size_t, size_t, size_t c, std::vector<real_t>& out) {
+      put_c(out, c, call_k(f, in, c, std::index_sequence_for<G...>{}));
+    });
+  }
+  template <typename F, typename... G>
+  void assign_function_of_grids_ijk(const F& f, G&... grids) {
+    const auto in = read_all(grids...);
+    each_k([&](size_t i, size_t j, size_t k, size_t c, std::vector<real_t>& out) {
+      put_c(out, c, call_k(f, in, c, std::index_sequence_for<G...>{}, std::array<size_t, 3>{i, j, k}));
+    });
+  }
+  template <typename F, typename... G>
+  void assign_function_of_grids_kdep(const F& f, G&... grids) {
+    const auto in = read_all(grids...);
+    each_k([&](size_t i, size_t j, size_t k, size_t c, std::vector<real_t>& out) {
+      put_c(out, c, call_k(f, in, c, std::index_sequence_for<G...>{}, get_k<real_t>(i, j, k)));
+    });
+  }
+
   /* single elements read from HBM (grid_fft.hh:179-211) */
   real_t relem(size_t i, size_t j, size_t k) const { return relem((i * n_[0] + j) * (n_[0] + 2) + k); }
   real_t relem(size_t idx) const {
@@ -258,6 +336,50 @@ class Grid_FFT {
 
  private:
   size_t stored_reals() const { return (n_[0] + 2) * n_[0] * n_[0]; }
+  static ccomplex_t get_c(const std::vector<real_t>& a, size_t c) { return ccomplex_t(a[2 * c], a[2 * c + 1]); }
+  static void put_c(std::vector<real_t>& a, size_t c, const ccomplex_t& v) {
+    a[2 * c] = v.real();
+    a[2 * c + 1] = v.imag();
+  }
+  /* loops of grid_fft.hh over sizes_[0..2] of the current space; B(i, j, k,
+   * element index, padded array), then the array goes back to the device */
+  template <typename B>
+  void each_k(const B& body) {
+    const space_t s = space();
+    std::vector<real_t> out;
+    download(out);
+    const size_t n = n_[0], nk = n / 2 + 1;
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j)
+        for (size_t k = 0; k < nk; ++k) body(i, j, k, (i * n + j) * nk + k, out);
+    upload(out, s);
+  }
+  template <typename B>
+  void each_r(const B& body) {
+    const space_t s = space();
+    std::vector<real_t> out;
+    download(out);
+    const size_t n = n_[0];
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j)
+        for (size_t k = 0; k < n; ++k) body(i, j, k, (i * n + j) * (n + 2) + k, out);
+    upload(out, s);
+  }
+  template <typename... G>
+  static std::array<std::vector<real_t>, sizeof...(G)> read_all(G&... grids) {
+    std::array<std::vector<real_t>, sizeof...(G)> in;
+    size_t q = 0;
+    (void)std::initializer_list<int>{(grids.download(in[q++]), 0)...};
+    return in;
+  }
+  template <typename F, typename A, size_t... I, typename... Lead>
+  static ccomplex_t call_k(const F& f, const A& in, size_t c, std::index_sequence<I...>, const Lead&... lead) {
+    return ccomplex_t(f(lead..., get_c(in[I], c)...));
+  }
+  template <typename F, typename A, size_t... I>
+  static real_t call_r(const F& f, const A& in, size_t r, std::index_sequence<I...>) {
+    return real_t(f(in[I][r]...));
+  }
   void read(size_t idx, size_t count, void* out, size_t bytes) const {
     if (idx >= count) throw std::out_of_range("Grid_FFT: element outside the stored layout");
     void* d = nullptr;

@@ -51,6 +51,32 @@ int run(mfgpu::context& ctx) {
   phi.download(padded);
   CHECK(padded.size() == (n + 2) * n * n && padded[phi.get_idx(5, 6, 7)] == real_t(x[(5 * n + 6) * n + 7]));
 
+  // functors on the host mirror, as ic_generator.cc:341-457 uses them
+  {
+    Grid_FFT<real_t> a(ctx, {n, n, n}, {L, L, L}), b(ctx, {n, n, n}, {L, L, L});
+    a.fill_real64(x);
+    const real_t a234 = a.relem(2, 3, 4);
+    a.apply_function_r_dep([](auto v, auto r) { return v + r.z; });
+    CHECK(a.relem(2, 3, 4) == a234 + real_t(4) * a.get_dx(2));
+    b.assign_function_of_grids_r([](auto u, auto w) { return u - w; }, a, a);
+    CHECK(b.relem(2, 3, 4) == real_t(0) && b.space() == mfgpu::rspace_id);
+    a.apply_function_r([](auto v) { return v * real_t(2); });
+    CHECK(a.relem(2, 3, 4) == (a234 + real_t(4) * a.get_dx(2)) * real_t(2));
+    a.FourierTransformForward();
+    const std::complex<real_t> c = a.kelem(1, 2, 3);
+    const auto k = a.template get_k<real_t>(1, 2, 3);
+    a.apply_function_k_dep([](auto v, auto kv) { return v * kv.norm_squared(); });
+    const std::complex<real_t> c2 = c * k.norm_squared();
+    CHECK(a.kelem(1, 2, 3) == c2 && a.space() == mfgpu::kspace_id);
+    b.assign_function_of_grids_kdep([](auto kv, auto u, auto w) { return u * w * kv.x; }, a, a);
+    CHECK(b.kelem(1, 2, 3) == c2 * c2 * k.x);
+    b.assign_function_of_grids_ijk([](auto ijk, auto u) { return u * real_t(ijk[0] + ijk[2]); }, a);
+    CHECK(b.kelem(1, 2, 3) == c2 * real_t(4));
+    b.assign_function_of_grids_k([](auto u) { return u + u; }, a);
+    b.apply_function_k([](auto v) { return std::conj(v); });
+    CHECK(b.kelem(1, 2, 3) == std::conj(c2 + c2));
+  }
+
   phi.FourierTransformForward();
   CHECK(phi.space() == mfgpu::kspace_id && phi.size(2) == n / 2 + 1 && phi.size(3) == n / 2 + 1);
   const std::complex<real_t> k123 = phi.kelem(1, 2, 3);
