@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from tests.ic_helpers import rel_l2, setup
+from tests.ic_helpers import lattice_q, rel_l2, setup
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +31,8 @@ def test_host_table_equals_device_fit(ctx):
     k = np.sqrt(np.arange(3 * (n // 2) ** 2 + 1, dtype=np.float64)) * (2.0 * math.pi / L)
     ref = _run(ctx, cfg, sc, noise)
     tab = _run(ctx, cfg, sc, noise, ic.eh_transfer(cosmo, k))
-    assert np.max(np.abs(tab[0] - ref[0])) < 1e-12 * L
+    q = lattice_q(n, 0, L)
+    assert rel_l2(tab[0] - q, ref[0] - q) < 1e-12
     assert rel_l2(tab[1], ref[1]) < 1e-12
     assert np.array_equal(tab[2], ref[2])
 
