@@ -136,3 +136,61 @@ def test_oracle_reproduces_the_lpt_fixture(mflib):
     q = lattice_q(n, lat, L)  # compare displacements: positions minus the lattice
     assert np.linalg.norm((pos - q) - (g["pos"] - q)) / np.linalg.norm(g["pos"] - q) < 1e-13
     assert np.linalg.norm(vel - g["vel"]) / np.linalg.norm(g["vel"]) < 1e-13
+
+
+# -- further invariants of the oracle ----------------------------------------
+def test_inverse_laplacian_inverts_the_laplacian():
+    """apply_InverseLaplacian (grid_fft.hh:440-449) undoes -k^2 except on the
+    zeroed DC mode"""
+    n, L = 16, 50.0
+    X = O.r2c(np.random.default_rng(2).standard_normal((n, n, n)))
+    kx, ky, kz = O.kgrids(n, L)
+    Y = O.inverse_laplacian(-(kx * kx + ky * ky + kz * kz) * X, L)
+    X0 = X.copy()
+    X0[0, 0, 0] = 0
+    assert Y[0, 0, 0] == 0 and np.allclose(Y, X0, rtol=1e-13, atol=1e-13)
+
+
+def test_shift_field_by_whole_cells_is_a_roll():
+    """shift_field (grid_fft.hh:832-842): a shift by whole cells moves the
+    field on the grid; a shift and its inverse restore it"""
+    n, L = 16, 50.0
+    x = np.random.default_rng(3).standard_normal((n, n, n))
+    assert np.allclose(O.shift_field(x, (1.0, 0.0, 2.0), L), np.roll(x, (-1, -2), axis=(0, 2)), atol=1e-12)
+    # the Nyquist planes of a half-cell shift lose their imaginary parts: compare band-limited fields
+    X = O.r2c(x)
+    X[n // 2] = 0
+    X[:, n // 2] = 0
+    X[:, :, n // 2] = 0
+    xb = O.c2r(X, n)
+    back = O.shift_field(O.shift_field(xb, (0.5, 0.25, -0.5), L), (-0.5, -0.25, 0.5), L)
+    assert np.allclose(back, xb, atol=1e-12)
+
+
+@pytest.mark.parametrize("lattice", [0, 1, 2, 3])
+def test_particle_ids_are_a_permutation(lattice):
+    """particle IDs of each lattice (particle_generator.hh:212-253): overload*cell + iload,
+    every ID exactly once, sub-lattice s occupying particles s*n^3 .. (s+1)*n^3-1"""
+    n = 8
+    overload = 1 << lattice
+    ids = O.particle_ids(n, lattice)
+    assert len(ids) == overload * n ** 3
+    assert np.array_equal(np.sort(ids), np.arange(overload * n ** 3, dtype=ids.dtype))
+    for s in range(overload):
+        assert np.all(ids[s * n ** 3:(s + 1) * n ** 3] % overload == s)
+    assert np.array_equal(O.particle_ids(n, lattice, id_offset=1) - ids, np.full(len(ids), overload * n ** 3))
+
+
+def test_naive_and_orszag_agree_on_band_limited_products():
+    """for fields whose product stays inside the grid's band the aliased
+    (NaiveConvolver) and dealiased (OrszagConvolver) products coincide"""
+    n = 16
+    i = np.arange(n)
+    xx = np.meshgrid(i, i, i, indexing="ij")
+    f = np.cos(2 * np.pi * 2 * xx[0] / n) + np.sin(2 * np.pi * 1 * xx[2] / n)
+    g = np.cos(2 * np.pi * 3 * xx[1] / n)
+    A, B = O.r2c(f), O.r2c(g)
+    assert np.allclose(O.naive_conv2(A, B), O.orszag_conv2(A, B), atol=1e-12)
+    h = np.sin(2 * np.pi * 1 * xx[0] / n)
+    C3 = O.r2c(h)
+    assert np.allclose(O.c2r(O.orszag_conv3(A, B, C3), n), f * g * h, atol=1e-12)
