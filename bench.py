@@ -50,7 +50,9 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="mf", choices=["mf", "reference"])
+    # "stub": the rank bookkeeping alone on gloo/CPU (no GPU work), for testing
+    # that --gpus N starts N ranks
+    ap.add_argument("--impl", default="mf", choices=["mf", "reference", "stub"])
     ap.add_argument("--ngrid", type=int, default=512)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -62,8 +64,9 @@ def parse():
     ap.add_argument("--batch-items", type=int, default=96)
     ap.add_argument("--batch-streams", type=int, default=8)
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=30.0)
-    ap.add_argument("--serve-seconds-fp64", type=float, default=6.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-seconds-fp64", type=float, default=60.0)
+    ap.add_argument("--detail", default=None, help="file for the full per-kernel / batch / serving detail")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-workers", type=int, default=4)
     return ap.parse_args()
@@ -230,7 +233,7 @@ def run_reference(args):
             vals.append(r)
     v = statistics.median([r["value"] for r in vals])
     ms = statistics.median([r["seconds_per_ic"] for r in vals]) * 1e3
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": _launched_world(), "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(n, 1) | {"reference_impl": "oracle port (numpy/scipy FP64 restatement of the "
@@ -418,7 +421,13 @@ def run_serve(args, device, prec, seconds):
     wait = [(r["t_admit"] - r["t_submit"]) * 1e3 for r in res]
     span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
     ok = sum(r["status"] == 0 for r in res)
+    # service capacity: completions over the span in which the server was busy;
+    # an arrival rate above it makes the queue (and p99) grow with the window
+    busy = max(r["t_done"] for r in res) - min(r["t_admit"] for r in res)
+    capacity = ok / busy if busy > 0 else None
+    overloaded = bool(capacity is not None and capacity < 0.95 * args.serve_rate)
     return {"precision": prec, "arrival_rate_per_s": args.serve_rate, "window_s": seconds, "requests": len(ids),
+            "capacity_req_per_s": round(capacity, 2) if capacity else None, "overloaded": overloaded,
             "completed": ok, "warmup_requests": nwarm, "workers": args.serve_workers,
             "latency_ms": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99), "max": max(lat)},
             "latency_to_device_done_ms": {"p50": _pct(lat_gpu, 0.5), "p99": _pct(lat_gpu, 0.99)},
@@ -620,38 +629,141 @@ def run_mf(args):
     if rank == 0:
         p50 = lat[len(lat) // 2]
         p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
+        roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic_per_launch(dom, n, 4)[0],
+                "traffic_source": traffic_per_launch(dom, n, 4)[1], "algorithmic_bytes_per_launch": bpl,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+        detail = {"kernels": kinds, "stages_ms": stages32, "autotuned_schedules": tuned or None, "e2e": e2e,
+                  "fp64_plain": fp64, "cpu_baseline": cpu, "clocks": clk, "batch": batch, "serving": serving,
+                  "output": output, "roofline": roof, "latency_ms": {"p50": p50, "p99": p99}}
+        detail_path = write_detail(args, detail)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(n, world),
-            "latency_ms": {"p50": p50, "p99": p99},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic_per_launch(dom, n, 4)[0],
-                         "traffic_source": traffic_per_launch(dom, n, 4)[1],
-                         "algorithmic_bytes_per_launch": bpl,
-                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"},
-            "kernels": kinds,
-            "stages_ms": stages32,
-            "autotuned_schedules": tuned or None,
-            "e2e": e2e,
-            "fp64_plain": fp64,
-            "cpu_baseline": cpu,
             "clocks": clk,
-            "batch": batch,
-            "serving": serving,
-            "output": output,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "roofline": roof,
+            "latency_ms": {"p50": round(p50, 3), "p99": round(p99, 3)},
+            "output": _short_output(output),
+            "batch": _short_batch(batch),
+            "serving": _short_serving(serving),
+            "stages_ms": stages32,
+            # per kind: GB/s over the IC's algorithmic bytes, fraction of measured HBM, ms per IC
+            "kernels": {k: [v["GB_s"], round(v["GB_s"] / peak, 3) if v["GB_s"] else None,
+                            round(v["ms_total"] / args.steps, 2)] for k, v in kinds.items()},
+            "fp64_plain": _short_fp64(fp64),
+            "detail_file": detail_path,
         }
         print(json.dumps(line))
     job.close()
     return 0
 
 
+def write_detail(args, detail) -> str | None:
+    """the full per-kernel, schedule, batch and serving record, too long for
+    the one printed line, goes to a side file"""
+    path = args.detail
+    if path is None:
+        out = os.path.join(ROOT, "gpurun_out")
+        path = os.path.join(out if os.path.isdir(out) else tempfile.gettempdir(), "bench_detail.json")
+    try:
+        with open(path, "w") as f:
+            json.dump(detail, f, indent=1)
+        return path
+    except OSError:
+        return None
+
+
+def _short_output(o):
+    if not o or "failed" in o:
+        return o
+    return {k: o[k] for k in ("write_GBps", "host_plain_write_GBps", "frac_of_host_write", "ic_plus_write_ms")}
+
+
+def _short_batch(b):
+    if not b:
+        return b
+    return {"items": sum(b["sizes"].values()), "ms_per_batch": round(b["ms_per_batch"], 2),
+            "particles_per_s": b["particles_per_s"], "realizations_per_s": round(b["realizations_per_s"], 1),
+            "graph_launches_per_batch": b["graph_launches_per_batch"], "kernels_per_batch": b["kernels_per_batch"]}
+
+
+def _short_serving(s):
+    if not s:
+        return s
+    out = {}
+    for prec, r in s.items():
+        if "latency_ms" not in r:
+            out[prec] = r
+            continue
+        out[prec] = {"window_s": r["window_s"], "rate": r["arrival_rate_per_s"], "requests": r["requests"],
+                     "p50_ms": round(r["latency_ms"]["p50"], 1), "p99_ms": round(r["latency_ms"]["p99"], 1),
+                     "served_req_per_s": round(r["requests_per_s"], 2),
+                     "capacity_req_per_s": r.get("capacity_req_per_s"), "overloaded": r.get("overloaded")}
+    return out
+
+
+def _short_fp64(f):
+    if not f:
+        return f
+    return {"value": f["value"], "ms_per_step": round(f["ms_per_step"], 2),
+            "speedup_fp32_bulk_vs_fp64": round(f["speedup_fp32_bulk_vs_fp64"], 2),
+            "fp64_fma_peak_tflops_measured": f["fp64_fma_peak_tflops_measured"]}
+
+
+def _launched_world() -> int:
+    """ranks of the job this process belongs to (1 outside a launcher)"""
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def relaunch_ranks(n: int) -> int:
+    """--gpus N > 1 outside a launcher: start N ranks of this command on one
+    node (torch.distributed.run, rendezvous on 127.0.0.1) and return the
+    launcher's exit status; every rank then reads RANK / WORLD_SIZE /
+    LOCAL_RANK from its environment."""
+    import socket
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
+def run_stub(args):
+    """the multi-rank bookkeeping of the GPU arm without a GPU: gloo ranks,
+    barrier, max-over-ranks timing and the whole-job rate; rank 0 prints the
+    line with the real world size"""
+    from monofonic_gb300 import replicas
+    job = replicas.init("gloo")
+    units = 1000.0 * args.steps
+    job.barrier()
+    t0 = time.perf_counter()
+    time.sleep(0.01 * (job.rank + 1))
+    dt = job.max_over_ranks(time.perf_counter() - t0)
+    rate = job.aggregate_rate(units, dt)
+    ranks = job.sum_over_ranks(1.0)
+    if job.rank == 0:
+        print(json.dumps({"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": job.world, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "none", "data": "synthetic",
+                          "impl": "stub", "ranks_joined": int(ranks), "config": {"workload": "stub"}}))
+    job.close()
+    return 0
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch_ranks(args.gpus)
     if args.impl == "reference":
         return run_reference(args)
+    if args.impl == "stub":
+        return run_stub(args)
     return run_mf(args)
 
 

@@ -103,6 +103,13 @@ int mf_autotune_reset(void);
  * and, for conv_z, the kernel (0 TMA-pipelined radix-8 plan, 1 direct-load
  * radix-4 plan) */
 int mf_schedule_set(int kind, int L, int prec, int occ, int variant);
+/* self-test of the bounded-wait path (no reference counterpart): one CTA
+ * waits on an mbarrier that nothing arrives on and no copy targets, polling
+ * at most `polls` times (1 .. 2^24); the wait runs out, the kernel records
+ * the error flag and returns, and the call reports it as MF_ERR_TIMEOUT the
+ * way a stalled asynchronous copy of a pipeline kernel would be.  The
+ * context stays usable afterwards. */
+int mf_selftest_bounded_wait(mf_ctx* ctx, long polls);
 /* 1 if grid size n is supported by the compiled kernels */
 int mf_grid_size_supported(int n);
 

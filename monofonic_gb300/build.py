@@ -2,13 +2,18 @@
 
 Every .cu/.cpp file under csrc/ is compiled by its own nvcc process (run in
 parallel), then linked into monofonic_gb300/libmfgpu.so.  Objects are cached
-under monofonic_gb300/_build/ keyed on the source and header timestamps.
+under monofonic_gb300/_build/, each keyed on a content hash of its source, of
+every header it may include, of the compiler flags and of the machine
+architecture; the library is relinked when the set of object keys changes.
+A copied tree with stale binaries (other machine, other flags, edited
+sources with older timestamps) therefore always recompiles what differs.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -37,12 +42,18 @@ def _sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
-def _headers_mtime():
-    ts = [os.path.getmtime(os.path.join(CSRC, f)) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+def _headers_digest():
+    """one digest over the contents of every header under csrc/ and include/"""
+    h = hashlib.sha256()
+    paths = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     inc = os.path.join(os.path.dirname(HERE), "include")
     if os.path.isdir(inc):
-        ts += [os.path.getmtime(os.path.join(inc, f)) for f in os.listdir(inc)]
-    return max(ts) if ts else 0.0
+        paths += [os.path.join(inc, f) for f in os.listdir(inc)]
+    for p in sorted(paths):
+        h.update(os.path.basename(p).encode())
+        with open(p, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
 
 
 def _objdir():
@@ -51,11 +62,30 @@ def _objdir():
     return os.path.join(BUILD, hashlib.sha1(" ".join(EXTRA).encode()).hexdigest()[:10])
 
 
-def _compile(src, nvcc, hdr_t, verbose):
+def _key(src, hdr_digest):
+    h = hashlib.sha256()
+    with open(os.path.join(CSRC, src), "rb") as f:
+        h.update(f.read())
+    h.update(hdr_digest.encode())
+    h.update(" ".join([*ARCH, *FLAGS, *EXTRA]).encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
+def _read(path):
+    try:
+        with open(path) as f:
+            return f.read()
+    except OSError:
+        return None
+
+
+def _compile(src, nvcc, hdr_digest, verbose):
     obj = os.path.join(_objdir(), os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), hdr_t):
-        return obj, None
+    key = _key(src, hdr_digest)
+    if os.path.exists(obj) and _read(obj + ".key") == key and not verbose:
+        return obj, key, None
     cmd = [nvcc, *ARCH, *FLAGS, *EXTRA, "-c", path, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc, "-x", "cu", *ARCH, *FLAGS, *EXTRA, "-c", path, "-o", obj]
@@ -63,28 +93,32 @@ def _compile(src, nvcc, hdr_t, verbose):
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        return obj, f"{' '.join(cmd)}\n{r.stdout}\n{r.stderr}"
-    return obj, None
+        return obj, key, f"{' '.join(cmd)}\n{r.stdout}\n{r.stderr}"
+    if verbose and r.stderr:
+        print(r.stderr)
+    with open(obj + ".key", "w") as f:
+        f.write(key)
+    return obj, key, None
 
 
 def build(verbose: bool = False, jobs: int | None = None) -> str:
     os.makedirs(_objdir(), exist_ok=True)
     nvcc = _nvcc()
-    hdr_t = _headers_mtime()
+    hdr = _headers_digest()
     srcs = _sources()
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
-    objs, errs = [], []
+    objs, keys, errs = [], [], []
     with cf.ThreadPoolExecutor(jobs) as ex:
-        for obj, err in ex.map(lambda s: _compile(s, nvcc, hdr_t, verbose), srcs):
+        for obj, key, err in ex.map(lambda s: _compile(s, nvcc, hdr, verbose), srcs):
             objs.append(obj)
+            keys.append(key)
             if err:
                 errs.append(err)
     if errs:
         raise RuntimeError("libmfgpu build failed:\n" + "\n".join(errs))
-    newest = max(os.path.getmtime(o) for o in objs)
-    stamp = LIB + ".flags"
-    same_flags = os.path.exists(stamp) and open(stamp).read() == " ".join(EXTRA)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest or not same_flags:
+    lib_key = hashlib.sha256("\n".join(keys).encode()).hexdigest()
+    stamp = LIB + ".key"
+    if not os.path.exists(LIB) or _read(stamp) != lib_key:
         tmp = LIB + ".tmp"
         cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -92,7 +126,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             raise RuntimeError("libmfgpu link failed:\n" + r.stdout + r.stderr)
         os.replace(tmp, LIB)
         with open(stamp, "w") as f:
-            f.write(" ".join(EXTRA))
+            f.write(lib_key)
     return LIB
 
 

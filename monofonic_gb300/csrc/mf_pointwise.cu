@@ -3,6 +3,7 @@
 #include <type_traits>
 
 #include "mf_noise.h"
+#include "mf_tma.cuh"
 #include "mf_runtime.h"
 
 namespace mf {
@@ -234,4 +235,33 @@ extern "C" int mf_probe_fma_rate(mf_ctx* c, int prec, double* tflops) {
   if (e != cudaSuccess) return mf::cuda_err(c, e, "mf_probe_fma_rate");
   *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
   return MF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// bounded-wait self-test: the failure path of every TMA-pipelined kernel
+// (mbar_wait_bounded) exercised without a fault.  One thread initialises an
+// mbarrier expecting one arrival; nothing arrives and no copy is issued, so
+// the phase never completes and the wait gives up after `polls` tries, sets
+// the context's error flag and returns.
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void k_wait_selftest(int* err, long polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mf::mbar_init(&bar, 1);
+    mf::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mf::mbar_wait_bounded_n(&bar, 0, err, 1, polls);
+}
+}  // namespace
+
+extern "C" int mf_selftest_bounded_wait(mf_ctx* c, long polls) {
+  if (!c) return MF_ERR_ARG;
+  if (polls < 1 || polls > (1L << 24)) return mf::set_err(c, MF_ERR_ARG, "mf_selftest_bounded_wait: polls out of range");
+  cudaSetDevice(c->device);
+  k_wait_selftest<<<1, 32, 0, c->stream>>>(c->d_err, polls);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return mf::cuda_err(c, e, "mf_selftest_bounded_wait");
+  return mf::check_device_error(c);
 }

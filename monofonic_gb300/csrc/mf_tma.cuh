@@ -56,6 +56,14 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return false;
 }
 
+// the same wait with a caller-chosen poll budget
+__device__ __forceinline__ bool mbar_wait_bounded_n(uint64_t* bar, unsigned parity, int* err, int code, long polls) {
+  for (long it = 0; it < polls; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicExch(err, code);
+  return false;
+}
+
 // per-thread asynchronous global -> shared copies (LDGSTS); completion is
 // tracked per thread with commit/wait groups (no spin loop involved)
 __device__ __forceinline__ void cp_async8(void* dst, const void* src) {

@@ -61,3 +61,20 @@ def test_reference_arm_prints_on_rank0_only():
                         "--warmup", "0"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_bench_gpus_2_starts_two_ranks():
+    """bench.py --gpus 2 outside a launcher starts two ranks itself (the stub
+    arm runs the GPU arm's rank bookkeeping on gloo) and reports the real
+    world size"""
+    import json
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE")}
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "stub", "--gpus", "2", "--steps", "3", "--warmup", "0"],
+                       cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["ranks_joined"] == 2
+    # both ranks' units over the slowest rank's time
+    assert d["value"] == pytest.approx(2 * 3000.0 / (d["ms_per_step"] * 3 / 1e3), rel=1e-9)

@@ -5,9 +5,11 @@ simulation code that runs the generator in-process while its own memory pool
 owns the device, or host code that must avoid the implicit synchronisation
 of cudaMalloc/cudaFree.  These tests call it through the C ABI and compare it
 with the allocating convolver entry point (mf_conv_convolve2) on the same
-inputs, two calls in a row, within the tolerances of the other convolution
-tests (FP64 rel-L2 1e-12, FP32 1e-5).  The file is named so that pytest runs
-it last.
+inputs and with the oracle's Orszag convolution, two calls in a row, within
+the tolerances of the other convolution tests (FP64 rel-L2 1e-12, FP32 1e-5),
+at the largest sizes the static scratch admits, and check that a call leaves
+the device's free memory unchanged.  The file is named so that pytest runs it
+last.
 """
 import ctypes as C
 
@@ -42,13 +44,25 @@ def _rel(a, b):
     return float(np.linalg.norm(a.astype(np.complex128) - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("prec", ["f64", "f32"])
-def test_noalloc_matches_allocating_convolver_twice(prec):
+def _free_device_bytes():
+    import torch
+    free, _ = torch.cuda.mem_get_info(0)
+    return free
+
+
+# (precision, n): the sizes at the edge of the 48 MiB scratch (FP64 n = 96,
+# 32.5 MB; FP32 n = 128, 38.3 MB), a small size for the first twiddle-table
+# offsets, and n = 64 in both precisions
+CASES = [("f64", 64), ("f32", 64), ("f64", 96), ("f32", 128), ("f32", 16)]
+
+
+@pytest.mark.parametrize("prec,n", CASES)
+def test_noalloc_matches_allocating_convolver_twice(prec, n):
     import monofonic_gb300 as mf
     fn = _entry()
     ctx = mf.Context(0)
-    n, L = 64, 100.0
-    rng = np.random.default_rng(11)
+    L = 100.0
+    rng = np.random.default_rng(11 + n)
     A = O.r2c(rng.standard_normal((n, n, n)))
     B = O.r2c(rng.standard_normal((n, n, n)))
     ga, gb = mf.Grid_FFT(ctx, n, L, prec, "k"), mf.Grid_FFT(ctx, n, L, prec, "k")
@@ -61,20 +75,33 @@ def test_noalloc_matches_allocating_convolver_twice(prec):
     cv.convolve_Hessians(ga, (1, 2), ga, (1, 2), mf.op.add_to(ref2))
     ctx.synchronize()
     want1, want2 = ref1.get_k(), ref2.get_k()
+    # the oracle's Orszag convolution of the same (device-rounded) operands
+    Ad, Bd = ga.get_k().astype(np.complex128), gb.get_k().astype(np.complex128)
+    orc1 = O.orszag_conv2(O.hessian(Ad, L, 0, 1), O.hessian(Bd, L, 2, 2))
+    orc2 = (O.orszag_conv2(O.hessian(Bd, L, 0, 0), O.sum_hessian(Ad, L, (1, 1), (2, 2)))
+            + O.orszag_conv2(O.hessian(Ad, L, 1, 2), O.hessian(Ad, L, 1, 2)))
 
     out = mf.Grid_FFT(ctx, n, L, prec, "k")
-    # first call: assign
+    # first call: assign (the first call on a device also looks up the scratch address)
     rc = fn(ctx.stream(), n, L, PREC[prec], ga.device_ptr(), MF_OPND_HESS, _dirs(0, 1), gb.device_ptr(),
             MF_OPND_HESS, _dirs(2, 2), out.device_ptr(), MF_OP_ASSIGN, 1.0)
     assert rc == 0
-    assert _rel(out.get_k(), want1) < TOL[prec]
-    # second call in a row, different operands, accumulated onto a prepared target
+    got1 = out.get_k()
+    assert _rel(got1, want1) < TOL[prec]
+    assert _rel(got1, orc1) < TOL[prec]
+    # second call in a row, different operands, accumulated onto a prepared
+    # target; it allocates no device memory
     cv.convolve_SumOfHessians(gb, (0, 0), ga, (1, 1), (2, 2), mf.op.assign_to(out))
     ctx.synchronize()
+    free0 = _free_device_bytes()
     rc = fn(ctx.stream(), n, L, PREC[prec], ga.device_ptr(), MF_OPND_HESS, _dirs(1, 2), ga.device_ptr(),
             MF_OPND_HESS, _dirs(1, 2), out.device_ptr(), MF_OP_ADD, 1.0)
     assert rc == 0
-    assert _rel(out.get_k(), want2) < TOL[prec]
+    ctx.synchronize()
+    assert _free_device_bytes() == free0
+    got2 = out.get_k()
+    assert _rel(got2, want2) < TOL[prec]
+    assert _rel(got2, orc2) < TOL[prec]
 
 
 def test_noalloc_rejects_sizes_beyond_its_static_scratch():
