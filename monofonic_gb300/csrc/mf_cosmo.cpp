@@ -7,9 +7,10 @@
 // include/math/ode_integrate.hh:39-111), log-log natural cubic-spline
 // interpolation of the tables (include/math/interpolate.hh:29-103), vfac
 // (cosmology_calculator.hh:360-363) and the sigma_8 normalisation
-// (cosmology_calculator.hh:368-380, 439-463).  The sigma_8 integral uses
-// adaptive 16-point Gauss-Legendre quadrature with nodes from Newton's method
-// in place of GSL's QAG-61 rule (same integral to ~1e-12 relative).
+// (cosmology_calculator.hh:368-380, 439-463).  The sigma_8 integral is the
+// same QAG with the 61-point Gauss-Kronrod rule to relative 1e-10 (mf_quad.h,
+// the rule computed rather than tabulated), so the scalars follow the
+// reference's to rounding.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -23,6 +24,7 @@
 #include "mf_cosmo.h"
 #include "mf_eh.cuh"
 #include "mf_noise.h"
+#include "mf_quad.h"
 
 namespace mf {
 
@@ -140,14 +142,20 @@ void growth_tables(const Cosmo& c, std::vector<double>& ta, std::vector<double>&
     V3 yscale;
     for (int i = 0; i < 3; ++i) yscale[i] = std::fabs(y[i]) + dt * std::fabs(f0[i]);
     double h = dt, hnext = dt;
+    // the trial state: each trial advances it in place, and a rejected trial
+    // is retried from the state it left behind, as the reference's
+    // rk_step_qs does (ckrk5_step updates ytemp, which is not reset before
+    // the retry; include/math/ode_integrate.hh:73-110)
+    V3 yt = y;
     for (;;) {
-      V3 k1 = rhs(y); for (auto& v : k1) v *= h;
-      V3 k2 = rhs(axpy(y, {{b21, &k1}})); for (auto& v : k2) v *= h;
-      V3 k3 = rhs(axpy(y, {{b31, &k1}, {b32, &k2}})); for (auto& v : k3) v *= h;
-      V3 k4 = rhs(axpy(y, {{b41, &k1}, {b42, &k2}, {b43, &k3}})); for (auto& v : k4) v *= h;
-      V3 k5 = rhs(axpy(y, {{b51, &k1}, {b52, &k2}, {b53, &k3}, {b54, &k4}})); for (auto& v : k5) v *= h;
-      V3 k6 = rhs(axpy(y, {{b61, &k1}, {b62, &k2}, {b63, &k3}, {b64, &k4}, {b65, &k5}})); for (auto& v : k6) v *= h;
-      V3 yt = axpy(y, {{c1, &k1}, {c3, &k3}, {c4, &k4}, {c6, &k6}});
+      const V3 base = yt;
+      V3 k1 = rhs(base); for (auto& v : k1) v *= h;
+      V3 k2 = rhs(axpy(base, {{b21, &k1}})); for (auto& v : k2) v *= h;
+      V3 k3 = rhs(axpy(base, {{b31, &k1}, {b32, &k2}})); for (auto& v : k3) v *= h;
+      V3 k4 = rhs(axpy(base, {{b41, &k1}, {b42, &k2}, {b43, &k3}})); for (auto& v : k4) v *= h;
+      V3 k5 = rhs(axpy(base, {{b51, &k1}, {b52, &k2}, {b53, &k3}, {b54, &k4}})); for (auto& v : k5) v *= h;
+      V3 k6 = rhs(axpy(base, {{b61, &k1}, {b62, &k2}, {b63, &k3}, {b64, &k4}, {b65, &k5}})); for (auto& v : k6) v *= h;
+      yt = axpy(base, {{c1, &k1}, {c3, &k3}, {c4, &k4}, {c6, &k6}});
       double errmax = 0.0;
       for (int i = 0; i < 3; ++i) {
         const double e = dc1 * k1[i] + dc3 * k3[i] + dc4 * k4[i] + dc5 * k5[i] + dc6 * k6[i];
@@ -208,61 +216,6 @@ class LogLogSpline {
   std::vector<double> x_, y_, m_;
 };
 
-// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n
-void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
-  x.resize(n); w.resize(n);
-  for (int i = 0; i < n; ++i) {
-    double z = std::cos(kPi * (i + 0.75) / (n + 0.5)), pp = 0;
-    for (int it = 0; it < 100; ++it) {
-      double p1 = 1.0, p2 = 0.0;
-      for (int j = 1; j <= n; ++j) { const double p3 = p2; p2 = p1; p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j; }
-      pp = n * (z * p1 - p2) / (z * z - 1.0);
-      const double z1 = z;
-      z = z1 - p1 / pp;
-      if (std::fabs(z - z1) < 1e-16) break;
-    }
-    x[i] = z;
-    w[i] = 2.0 / ((1.0 - z * z) * pp * pp);
-  }
-}
-
-double integrate_adaptive(const std::function<double(double)>& f, double a, double b, double rtol) {
-  static std::vector<double> gx, gw;
-  if (gx.empty()) gauss_legendre(16, gx, gw);
-  auto gl = [&](double lo, double hi) {
-    const double c = 0.5 * (lo + hi), r = 0.5 * (hi - lo);
-    double s = 0;
-    for (size_t i = 0; i < gx.size(); ++i) s += gw[i] * f(c + r * gx[i]);
-    return s * r;
-  };
-  // integrate in pieces evenly spaced in log k, then refine each piece by
-  // bisection until the change is below rtol times the whole integral
-  const int pieces = 160;
-  std::vector<std::array<double, 4>> stack;  // lo, hi, estimate, depth
-  double coarse = 0;
-  for (int p = 0; p < pieces; ++p) {
-    const double lo = a * std::pow(b / a, double(p) / pieces), hi = a * std::pow(b / a, double(p + 1) / pieces);
-    const double v = gl(lo, hi);
-    coarse += v;
-    stack.push_back({lo, hi, v, 0.0});
-  }
-  const double atol = rtol * std::fabs(coarse) / pieces;
-  double total = 0;
-  while (!stack.empty()) {
-    auto seg = stack.back();
-    stack.pop_back();
-    const double mid = 0.5 * (seg[0] + seg[1]);
-    const double l = gl(seg[0], mid), r = gl(mid, seg[1]);
-    if (std::fabs(l + r - seg[2]) <= atol || seg[3] >= 30) {
-      total += l + r;
-    } else {
-      stack.push_back({seg[0], mid, l, seg[3] + 1});
-      stack.push_back({mid, seg[1], r, seg[3] + 1});
-    }
-  }
-  return total;
-}
-
 }  // namespace
 }  // namespace mf
 
@@ -307,7 +260,13 @@ extern "C" int mf_cosmology_compute(const mf_cosmo_params* p, double zstart, mf_
     const double tk = eh_eval(eh, k);
     return k * k * w * w * std::pow(k, ns) * tk * tk;
   };
-  const double sigma0 = 4.0 * M_PI * integrate_adaptive(dsig, 1e-4, 1e4, 1e-13);
+  // the reference's integrate(): QAG with the 61-point Gauss-Kronrod rule to
+  // relative 1e-10 over the transfer plugin's [kmin, kmax] = [1e-4, 1e4]
+  // (cosmology_calculator.hh:62-83, 439-452; transfer_eisenstein.cc:243-251)
+  static const quad::GKRule gk61 = quad::make_rule(30);
+  double sig_int = 0.0, sig_err = 0.0;
+  quad::qag(gk61, dsig, 1e-4, 1e4, 0.0, 1e-10, 100000, &sig_int, &sig_err);
+  const double sigma0 = 4.0 * M_PI * sig_int;
   out->sigma8_measured = std::sqrt(sigma0);
   out->pnorm = c.sigma8 * c.sigma8 / (out->sigma8_measured * out->sigma8_measured);
   out->n_s = ns;

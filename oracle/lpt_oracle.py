@@ -204,14 +204,19 @@ def _growth_table(p):
     while y[0] < 2.0:
         yscale = np.abs(y) + dt * np.abs(rhs(y))
         h = dt
+        # rk_step_qs advances its trial state ytemp in place and retries a
+        # rejected step from the state that trial left behind
+        # (include/math/ode_integrate.hh:73-110: ytemp is not reset)
+        ytmp = y.copy()
         while True:
-            k1 = h * rhs(y)
-            k2 = h * rhs(y + c["b21"] * k1)
-            k3 = h * rhs(y + c["b31"] * k1 + c["b32"] * k2)
-            k4 = h * rhs(y + c["b41"] * k1 + c["b42"] * k2 + c["b43"] * k3)
-            k5 = h * rhs(y + c["b51"] * k1 + c["b52"] * k2 + c["b53"] * k3 + c["b54"] * k4)
-            k6 = h * rhs(y + c["b61"] * k1 + c["b62"] * k2 + c["b63"] * k3 + c["b64"] * k4 + c["b65"] * k5)
-            ytmp = y + c["c1"] * k1 + c["c3"] * k3 + c["c4"] * k4 + c["c6"] * k6
+            base = ytmp
+            k1 = h * rhs(base)
+            k2 = h * rhs(base + c["b21"] * k1)
+            k3 = h * rhs(base + c["b31"] * k1 + c["b32"] * k2)
+            k4 = h * rhs(base + c["b41"] * k1 + c["b42"] * k2 + c["b43"] * k3)
+            k5 = h * rhs(base + c["b51"] * k1 + c["b52"] * k2 + c["b53"] * k3 + c["b54"] * k4)
+            k6 = h * rhs(base + c["b61"] * k1 + c["b62"] * k2 + c["b63"] * k3 + c["b64"] * k4 + c["b65"] * k5)
+            ytmp = base + c["c1"] * k1 + c["c3"] * k3 + c["c4"] * k4 + c["c6"] * k6
             yerr = c["dc1"] * k1 + c["dc3"] * k3 + c["dc4"] * k4 + c["dc5"] * k5 + c["dc6"] * k6
             errmax = float(np.max(np.abs(yerr / yscale))) / eps
             if errmax > 1.0:
