@@ -125,6 +125,25 @@ class capture_output_plugin : public output_plugin {
         for (size_t k = 0; k < n2; ++k) v[(i * n1 + j) * n2 + k] = g.relem(i, j, k);
     write_npy(fname_ + "/" + species_name(s) + "_" + component_name(c) + ".npy", v.data(), v.size(), "<f8",
               {n0, n1, n2});
+    if (c == fluid_component::density) {
+      // the reference's own power-spectrum estimator on a copy of the field,
+      // at full precision (Grid_FFT::Compute_PowerSpectrum, src/grid_fft.cc:1133-1210)
+      Grid_FFT<real_t> cp({n0, n1, n2}, {g.length_[0], g.length_[1], g.length_[2]});
+      for (size_t i = 0; i < n0; ++i)
+        for (size_t j = 0; j < n1; ++j)
+          for (size_t k = 0; k < n2; ++k) cp.relem(i, j, k) = g.relem(i, j, k);
+      std::vector<double> bk, bp, be;
+      std::vector<size_t> bc;
+      cp.Compute_PowerSpectrum(bk, bp, be, bc);
+      std::vector<double> tab;
+      for (size_t b = 0; b < bk.size(); ++b) {
+        tab.push_back(bk[b]);
+        tab.push_back(bp[b]);
+        tab.push_back(be[b]);
+        tab.push_back((double)bc[b]);
+      }
+      write_npy(fname_ + "/" + species_name(s) + "_pk.npy", tab.data(), tab.size(), "<f8", {bk.size(), 4});
+    }
   }
 
   output_type write_species_as(const cosmo_species& s) const override {

@@ -120,22 +120,23 @@ def test_host_noise_golden_fixture(mflib):
     assert np.allclose(ref, O.white_noise(16, 12345), rtol=1e-14, atol=1e-14)
 
 
-def test_oracle_reproduces_the_lpt_fixture(mflib):
-    """the committed 3LPT BCC particles (tests/golden/make_lpt_fixture.py) are
-    what the oracle computes today: a change to the oracle shows up here"""
-    from monofonic_gb300 import ic
-    from tests.ic_helpers import setup
-    g = np.load(os.path.join(ROOT, "tests", "golden", "lpt3_bcc_n16_seed777.npz"))
-    n, L, z, order, lat = int(g["n"]), float(g["boxlen"]), float(g["zstart"]), int(g["order"]), int(g["lattice"])
-    _, sc, osc = setup(z)
-    assert math.isclose(sc.Dplus, float(g["Dplus"]), rel_tol=1e-14)
-    f = O.lpt_potentials(ic.white_noise(n, int(g["seed"])), L, order, osc)
-    pos, vel, ids = O.particles(f, L, order, osc.vfac, lattice=lat, lunit=L, vunit=L)
-    assert np.array_equal(ids, g["ids"])
-    from tests.ic_helpers import lattice_q
-    q = lattice_q(n, lat, L)  # compare displacements: positions minus the lattice
-    assert np.linalg.norm((pos - q) - (g["pos"] - q)) / np.linalg.norm(g["pos"] - q) < 1e-13
-    assert np.linalg.norm(vel - g["vel"]) / np.linalg.norm(g["vel"]) < 1e-13
+@pytest.mark.parametrize("name", ["lpt3_bcc_n16", "lpt2_sc_naive_fixinv_n16", "fields_baryons_eulerian_lpt2_sc_n16"])
+def test_oracle_reproduces_the_reference_fixture(mflib, name):
+    """the reference's own output (tests/golden/ref_<case>.npz, written by
+    tests/golden/make_ref_fixtures.py from oracle/_ref) is what the oracle
+    computes from the same noise and scalars, to 1e-12; runs without the
+    reference's sources"""
+    from tests import ref_cases as R
+    case, scalars, want = R.load_fixture(name)
+    got = R.to_fixture_keys(case, R.oracle_outputs(case, scalars))
+    for key, w in want.items():
+        if key.endswith("_pk"):
+            continue
+        g = got[key]
+        if w.dtype.kind in "ui":
+            assert np.array_equal(g.astype(w.dtype), w), key
+        else:
+            assert np.linalg.norm(g - w) / np.linalg.norm(w) < 1e-12, key
 
 
 # -- further invariants of the oracle ----------------------------------------

@@ -75,21 +75,6 @@ def test_particles_f64(ctx, lattice, order):
 O_LAT = {"sc": 0, "bcc": 1, "fcc": 2, "rsc": 3}
 
 
-def test_particles_match_the_golden_fixture(ctx):
-    """the committed 3LPT BCC particles (tests/golden/make_lpt_fixture.py)"""
-    import os
-    from monofonic_gb300 import ic
-    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "lpt3_bcc_n16_seed777.npz"))
-    n, L, z, order = int(g["n"]), float(g["boxlen"]), float(g["zstart"]), int(g["order"])
-    cosmo, sc, osc = setup(z)
-    cfg = ic.ICConfig(ngrid=n, boxlen=L, zstart=z, lpt_order=order, lattice="bcc", lunit=L, vunit=L)
-    _, (pos, vel, ids) = run_gpu(ctx, cfg, sc, ic.white_noise(n, int(g["seed"])))
-    q = lattice_q(n, int(g["lattice"]), L)
-    assert rel_l2(pos - q, g["pos"] - q) < F64_TOL
-    assert rel_l2(vel, g["vel"]) < F64_TOL
-    assert np.array_equal(ids, g["ids"])
-
-
 def test_ids_u32_and_float_positions(ctx):
     from monofonic_gb300 import ic
     n, L, z = 16, 50.0, 30.0
