@@ -237,16 +237,64 @@ __host__ __device__ constexpr int plan_lcur(int L, int maxr, int s) {
   int p = 1; for (int i = 0; i < s; ++i) p *= plan_radix(L, maxr, i); return p;
 }
 
-// padded shared-memory index: one spare element per 16 (128 B of float2),
-// which makes every exchange of a radix-8-first plan free of bank conflicts
-// when a line's elements are contiguous in shared memory (stride 1)
-template <bool PAD>
-__device__ __forceinline__ int pidx(int e) { return PAD ? e + (e >> 4) : e; }
-__host__ __device__ constexpr int padded_len(int L, bool pad) { return pad ? L + (L >> 4) + 1 : L; }
+// Shared-memory layouts of the exchange buffer: element e of a line is kept
+// at slot pidx<LAYOUT>(e) (times the element stride of the caller).
+//   0  identity
+//   1  one spare slot per 16 elements (e + e/16)
+//   2  rows of a strided column tile: e ^ (bit 3 of e) in bit 0 -- with 8
+//      columns of 8-byte elements per row this makes every exchange of the
+//      radix-8-first plans take the minimum number of shared-memory
+//      wavefronts (two 64-byte rows per half-warp land in different banks)
+//   12, 13  XOR swizzles e ^ ((e >> s) & 15), s = 2 or 3, for contiguous
+//      lines whose length is a multiple of 16 (a bijection on [0, L): only
+//      the low four bits change, from higher bits)
+// The layout of a contiguous-line exchange is picked per length (zlayout)
+// from a count of shared-memory wavefronts per exchange instruction
+// (16 lanes of 8-byte accesses per wavefront, 32 four-byte banks) over every
+// write_out/read_in of the plan: the XOR swizzles reach the minimum for the
+// radix-8-first plans of lengths 16..384 that are multiples of 16, where
+// layout 1 takes up to twice as many for some exchanges.
+template <int LAYOUT>
+__device__ __forceinline__ int pidx(int e) {
+  if constexpr (LAYOUT == 1) return e + (e >> 4);
+  else if constexpr (LAYOUT == 2) return e ^ ((e >> 3) & 1);
+  else if constexpr (LAYOUT == 12) return e ^ ((e >> 2) & 15);
+  else if constexpr (LAYOUT == 13) return e ^ ((e >> 3) & 15);
+  else return e;
+}
+__host__ __device__ constexpr int padded_len(int L, int layout) { return layout == 1 ? L + (L >> 4) + 1 : L; }
+// exchange layout of a contiguous line of length L
+__host__ __device__ constexpr int zlayout(int L) {
+  return (L == 16 || L == 32 || L == 48 || L == 96 || L == 128 || L == 256 || L == 288 || L == 384 || L == 768)
+             ? 13
+             : ((L == 64 || L == 192) ? 12 : 1);
+}
+// distance between consecutive lines' exchange buffers (elements): the
+// layout's length, widened where it moves the lines of one half-warp onto
+// different banks
+__host__ __device__ constexpr int zline_stride(int L) {
+  switch (L) {
+    case 16: return 18;
+    case 24: return 27;
+    case 32: return 36;
+    case 48: return 50;
+    case 64: return 65;
+    case 96: return 100;
+    case 144: return 155;
+    case 192: return 193;
+    case 288: return 292;
+    default: return padded_len(L, zlayout(L)) | ((zlayout(L) == 1) ? 1 : 0);
+  }
+}
 
 // Line FFT of length L in precision T, direction INV, radices up to MAXR;
-// PAD selects the padded shared-memory index for contiguous (stride-1) lines.
-template <typename T, int L, bool INV, int MAXR = 8, bool PAD = false>
+// LAYOUT selects the shared-memory exchange index (pidx).  HOIST: a stage
+// whose butterflies of one thread all share k = t mod LC (TPL a multiple of
+// LC) loads its twiddles once instead of once per butterfly -- fewer L1
+// loads, but the twiddles stay live across the butterflies, so it is for
+// kernels with registers to spare (the strided passes at 128 registers
+// spill with it).
+template <typename T, int L, bool INV, int MAXR = 8, int LAYOUT = 0, bool HOIST = false>
 struct LineFFT {
   static_assert(plan_ok(L), "FFT length must be 2^a 3^b >= 4");
   using C = cplx<T>;
@@ -270,6 +318,22 @@ struct LineFFT {
     constexpr int R = plan_radix(L, MAXR, S);
     constexpr int LC = plan_lcur(L, MAXR, S);
     constexpr int NB = E / R;
+    if constexpr (HOIST && LC > 1 && TPL % LC == 0) {
+      // every butterfly of this thread has the same k = t mod LC: one set of
+      // twiddles for all of them
+      constexpr int STR = L / (LC * R);
+      const int k = t % LC;
+      C w[R];
+#pragma unroll
+      for (int p = 1; p < R; ++p) w[p] = tw[p * k * STR];
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+#pragma unroll
+        for (int p = 1; p < R; ++p) v[m * R + p] = INV ? cmulc(v[m * R + p], w[p]) : cmul(v[m * R + p], w[p]);
+        dftR<T, INV, R>(&v[m * R]);
+      }
+      return;
+    }
 #pragma unroll
     for (int m = 0; m < NB; ++m) {
       if constexpr (LC > 1) {
@@ -298,7 +362,7 @@ struct LineFFT {
       const int k = b % LC;
       const int base = (b - k) * R + k;
 #pragma unroll
-      for (int q = 0; q < R; ++q) sm[pidx<PAD>(base + q * LC) * cs] = v[m * R + q];
+      for (int q = 0; q < R; ++q) sm[pidx<LAYOUT>(base + q * LC) * cs] = v[m * R + q];
     }
   }
 
@@ -311,7 +375,7 @@ struct LineFFT {
     for (int m = 0; m < NB; ++m) {
       const int b = t + m * TPL;
 #pragma unroll
-      for (int p = 0; p < R; ++p) v[m * R + p] = sm[pidx<PAD>(b + p * (L / R)) * cs];
+      for (int p = 0; p < R; ++p) v[m * R + p] = sm[pidx<LAYOUT>(b + p * (L / R)) * cs];
     }
   }
 

@@ -53,6 +53,22 @@ __host__ __device__ constexpr int col_minb(int threads, int e, int scalar_bytes)
   return b < 1 ? 1 : (b > 4 ? 4 : b);
 }
 
+// exchange layout of a pipelined strided tile [row e][NCOL columns]: the
+// row swizzle (pidx<2>) where a row is 64 bytes (8 FP32 or 4 FP64 complex
+// columns) and the op asks for it (kColSwizzle), identity otherwise.  The
+// swizzle's per-element address arithmetic costs registers: the ops with a
+// prologue or a prefetched read-modify-write target (x passes) sit at the
+// 128-register cap of two CTAs per SM and would spill, so they keep the
+// identity layout.
+template <class OP, class = void>
+struct col_swizzle : std::false_type {};
+template <class OP>
+struct col_swizzle<OP, std::void_t<decltype(OP::kColSwizzle)>> : std::integral_constant<bool, OP::kColSwizzle> {};
+template <typename T, int NCOL, class OP>
+__host__ __device__ constexpr int col_layout() {
+  return (col_swizzle<OP>::value && NCOL * (int)sizeof(cplx<T>) == 64) ? 2 : 0;
+}
+
 // ops with a per-tile prologue (tile_prep / xform_tile) in the pipelined pass
 template <class OP, class = void>
 struct has_tile_prep : std::false_type {};
@@ -148,7 +164,8 @@ __global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
                                   col_minb(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
                                            LineFFT<T, L, INV, MF_COL_MAXR>::E, (int)sizeof(T)))
 k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
-  using F = LineFFT<T, L, INV, MF_COL_MAXR>;
+  constexpr int LAY = col_layout<T, NCOL, OP>();
+  using F = LineFFT<T, L, INV, MF_COL_MAXR, LAY>;
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf0 = reinterpret_cast<C*>(smem_raw);
@@ -161,7 +178,7 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 #pragma unroll
     for (int s = 0; s < F::E; ++s) {
       const int e = F::in_index(t, s);
-      C* d = buf + e * NCOL + c;
+      C* d = buf + pidx<LAY>(e) * NCOL + c;
       const C* g = (col < ncols) ? op.srcp(z, slab, e, col) : nullptr;
       if (g) {
         if constexpr (sizeof(C) == 16) cp_async16(d, g); else cp_async8(d, g);
@@ -188,13 +205,13 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 #pragma unroll
       for (int s = 0; s < F::E; ++s) {
         const int e = F::in_index(t, s);
-        v[s] = valid ? op.xform_tile(tp, e, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+        v[s] = valid ? op.xform_tile(tp, e, cur[pidx<LAY>(e) * NCOL + c]) : mkc<T>(T(0), T(0));
       }
     } else {
 #pragma unroll
       for (int s = 0; s < F::E; ++s) {
         const int e = F::in_index(t, s);
-        v[s] = valid ? op.xform(z, slab, e, col, cur[e * NCOL + c]) : mkc<T>(T(0), T(0));
+        v[s] = valid ? op.xform(z, slab, e, col, cur[pidx<LAY>(e) * NCOL + c]) : mkc<T>(T(0), T(0));
       }
     }
     if constexpr (OP::kPrefetch) {
@@ -227,8 +244,9 @@ __global__ void __launch_bounds__(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
                                   col_minb(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
                                            LineFFT<T, L, false, MF_COL_MAXR>::E, (int)sizeof(T)))
 k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
-  using FF = LineFFT<T, L, false, MF_COL_MAXR>;
-  using FI = LineFFT<T, L, true, MF_COL_MAXR>;
+  constexpr int LAY = col_layout<T, NCOL, ConvXTruncOp<T>>();
+  using FF = LineFFT<T, L, false, MF_COL_MAXR, LAY>;
+  using FI = LineFFT<T, L, true, MF_COL_MAXR, LAY>;
   static_assert(FF::E == FI::E && FF::TPL == FI::TPL, "one plan for both directions");
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -242,7 +260,7 @@ k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, in
 #pragma unroll
     for (int s = 0; s < FF::E; ++s) {
       const int e = FF::in_index(t, s);
-      C* d = buf + e * NCOL + c;
+      C* d = buf + pidx<LAY>(e) * NCOL + c;
       if (col < ncols) {
         if constexpr (sizeof(C) == 16) cp_async16(d, op.at(slab, e, col)); else cp_async8(d, op.at(slab, e, col));
       } else {
@@ -264,17 +282,17 @@ k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, in
     const bool valid = col < ncols;
     C v[FF::E];
 #pragma unroll
-    for (int s = 0; s < FF::E; ++s) v[s] = cur[FF::in_index(t, s) * NCOL + c];
+    for (int s = 0; s < FF::E; ++s) v[s] = cur[pidx<LAY>(FF::in_index(t, s)) * NCOL + c];
     FF::run(v, t, cur + c, NCOL, tw, SyncBlock{});
     __syncthreads();  // the last exchange of the forward transform has been read
 #pragma unroll
     for (int s = 0; s < FF::E; ++s) {
       const int e = FF::out_index(t, s);
-      cur[e * NCOL + c] = op.mask(slab, e, col, v[s]);
+      cur[pidx<LAY>(e) * NCOL + c] = op.mask(slab, e, col, v[s]);
     }
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < FI::E; ++s) v[s] = cur[FI::in_index(t, s) * NCOL + c];
+    for (int s = 0; s < FI::E; ++s) v[s] = cur[pidx<LAY>(FI::in_index(t, s)) * NCOL + c];
     FI::run(v, t, cur + c, NCOL, tw, SyncBlock{});
     if (valid) {
 #pragma unroll
@@ -613,13 +631,14 @@ __device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin,
 // MODE 2: the forward transform of one real line (H packed pairs, kin = H),
 //         stored as kz < kout like MODE 0.
 template <typename T, int H, int MAXR, int LPB, class SYNC, int MODE = 0>
-__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR, true>::TPL)
+__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL)
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
-  using FI = LineFFT<T, H, true, MAXR, true>;
-  using FF = LineFFT<T, H, false, MAXR, true>;
+  constexpr int LAY = zlayout(H);
+  using FI = LineFFT<T, H, true, MAXR, LAY, true>;
+  using FF = LineFFT<T, H, false, MAXR, LAY, true>;
   using C = cplx<T>;
   constexpr int E = FI::E, TPL = FI::TPL;
-  constexpr int LS = padded_len(H, true);  // padded per-line exchange length
+  constexpr int LS = zline_stride(H);  // per-line exchange length
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
   const int nop = a.nop, kin = a.kin;
@@ -692,20 +711,20 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
       if constexpr (MODE == 0) {
         sync();
 #pragma unroll
-        for (int s = 0; s < E; ++s) sm[pidx<true>(FI::out_index(t, s))] = prod[s];
+        for (int s = 0; s < E; ++s) sm[pidx<LAY>(FI::out_index(t, s))] = prod[s];
         sync();
 #pragma unroll
-        for (int s = 0; s < E; ++s) v[s] = sm[pidx<true>(FF::in_index(t, s))];
+        for (int s = 0; s < E; ++s) v[s] = sm[pidx<LAY>(FF::in_index(t, s))];
       }
       FF::run(v, t, sm, 1, twH, sync);
       sync();
 #pragma unroll
-      for (int s = 0; s < E; ++s) sm[pidx<true>(FF::out_index(t, s))] = v[s];
+      for (int s = 0; s < E; ++s) sm[pidx<LAY>(FF::out_index(t, s))] = v[s];
       sync();
       C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
       for (int k = t; k < a.kout; k += TPL) {
-        const C zk = sm[pidx<true>(k % H)];
-        const C zc = cconj(sm[pidx<true>((H - k) % H)]);
+        const C zk = sm[pidx<LAY>(k % H)];
+        const C zc = cconj(sm[pidx<LAY>((H - k) % H)]);
         const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
         const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
         dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);

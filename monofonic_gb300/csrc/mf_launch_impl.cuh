@@ -162,7 +162,7 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
   if (sc.variant == 0 || MODE != 0) {
     // TMA path: radix-8-first plan with the padded (conflict-free) exchange layout
     constexpr int MAXR = MF_ZCONV_TMA_MAXR;
-    constexpr int TPL = LineFFT<T, H, true, MAXR, true>::TPL;
+    constexpr int TPL = LineFFT<T, H, true, MAXR>::TPL;
     constexpr bool WARP = (TPL <= 32) && (32 % TPL == 0);
     using SYNC = typename std::conditional<WARP, SyncWarp, SyncBlock>::type;
     // lines per batch; the one-transform modes may use a fraction of it (a
@@ -176,7 +176,7 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     if (tma_ok) {
       auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE>;
       const size_t smem =
-          128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * padded_len(H, true)) * sizeof(cplx<T>);
+          128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * zline_stride(H)) * sizeof(cplx<T>);
       cudaError_t e = set_smem(kern, smem);
       if (e != cudaSuccess) return e;
       int per_sm = 0, nsm = 0, dev = 0;

@@ -183,6 +183,7 @@ struct ConvYInvOp {
   C* dst[3];        // same buffers, rows y < M (in place per slab)
   ConvGeom g;
   static constexpr bool kPrefetch = false;
+  static constexpr bool kColSwizzle = true;  // bank-conflict-free exchange rows (registers to spare)
   __device__ __forceinline__ C load(int x, int y, int kz) const {
     const int j = g.src_row(y);
     if (j < 0) return mkc<T>(T(0), T(0));
@@ -217,6 +218,7 @@ struct ConvYFwdOp {
   C* dst;        // same buffer, compact rows j < N (in place per slab)
   ConvGeom g;
   static constexpr bool kPrefetch = false;
+  static constexpr bool kColSwizzle = true;  // bank-conflict-free exchange rows (registers to spare)
   __device__ __forceinline__ C load(int x, int y, int kz) const {
     return src[((long long)x * g.M + y) * g.Kz + kz];
   }
