@@ -615,6 +615,10 @@ def run_mf(args):
         ctx.synchronize()
         wall_ms = (time.perf_counter() - w0) * 1e3 / args.steps
         t = max_over_ranks(e0.elapsed_time(e1))
+        # the part of the last step after its last kernel: the streamed
+        # particle copies still in flight (the copy engine runs at the box's
+        # pinned-copy rate; the slices become final only in the assembly)
+        handoff_tail_ms = gen32.stage_times()[7]
         ids_h = ids.array(np.uint64, (npart,))
         assert ids_h[1] == 2 and ids_h[n ** 3] == 1, "particle IDs wrong after e2e run"
         # the box's raw device-to-host copy rate into page-locked memory, for context
@@ -630,7 +634,8 @@ def run_mf(args):
                "h2d_bytes_per_step": int(noise_h.nbytes),
                "d2h_bytes_per_step": int(gen32.pos_bytes + gen32.vel_bytes + gen32.id_bytes),
                "ms_per_step": t / args.steps, "wall_ms_per_step": wall_ms,
-               "box_d2h_GBps_pinned_1GiB": round((1 << 30) / best / 1e9, 1)}
+               "box_d2h_GBps_pinned_1GiB": round((1 << 30) / best / 1e9, 1),
+               "handoff_tail_ms_last_step": round(handoff_tail_ms, 2)}
         for b in (pin_noise, pos, vel, ids):
             b.close()
     gen32.close()

@@ -110,6 +110,15 @@ int mf_schedule_set(int kind, int L, int prec, int occ, int variant);
  * way a stalled asynchronous copy of a pipeline kernel would be.  The
  * context stays usable afterwards. */
 int mf_selftest_bounded_wait(mf_ctx* ctx, long polls);
+/* self-test of the FP32-bulk form's float-pair arithmetic (no reference
+ * counterpart; the reference evaluates the order sum of ic_generator.cc:835-845
+ * and q + Psi of particle_generator.hh:524-541 in real_t): on `count`
+ * pseudo-random inputs shaped like the pipeline's, the device helpers that
+ * the order sum and the lattice readout use are compared with the FP64
+ * evaluation rounded once; *mism_sum / *mism_q receive the numbers of stored
+ * floats that differ.  Dplus sets the growth weights. */
+int mf_selftest_float_pairs(mf_ctx* ctx, long long count, uint64_t seed, double Dplus, long long* mism_sum,
+                            long long* mism_q);
 /* 1 if grid size n is supported by the compiled kernels */
 int mf_grid_size_supported(int n);
 

@@ -37,6 +37,8 @@ SIGNATURES = {
     "mf_ctx_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "mf_probe_fma_rate": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "mf_selftest_bounded_wait": (C.c_int, [C.c_void_p, C.c_long]),
+    "mf_selftest_float_pairs": (C.c_int, [C.c_void_p, C.c_longlong, C.c_uint64, C.c_double, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_longlong)]),
     "mf_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "mf_host_free": (C.c_int, [C.c_void_p]),
     "mf_grid_size_supported": (C.c_int, [C.c_int]),

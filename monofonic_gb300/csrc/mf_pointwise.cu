@@ -265,3 +265,78 @@ extern "C" int mf_selftest_bounded_wait(mf_ctx* c, long polls) {
   if (e != cudaSuccess) return mf::cuda_err(c, e, "mf_selftest_bounded_wait");
   return mf::check_device_error(c);
 }
+
+// ---------------------------------------------------------------------------
+// float-pair self-test: the FP32-bulk form carries the growth-weighted order
+// sum (k_phitot) and the lattice positions q + Psi (lattice readout) as float
+// pairs instead of FP64.  This kernel runs the same device helpers (ff_axpy,
+// ff_add_q) on `count` pseudo-random inputs shaped like the pipeline's
+// (three FP32 order terms with FP64 growth weights of z_start = 24; q a
+// lattice coordinate times the box length, Psi an FP32 displacement) and
+// counts the stored floats that differ from the FP64 evaluation rounded once.
+// ---------------------------------------------------------------------------
+namespace {
+__device__ __forceinline__ uint64_t sm64(uint64_t x) {  // splitmix64 finaliser
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+__device__ __forceinline__ float unit_f(uint64_t h) {  // uniform in (-1, 1), 24 random bits
+  return ((float)(h >> 40) + 0.5f) * (1.0f / 8388608.0f) - 1.0f;
+}
+__global__ void k_float_pair_selftest(long long count, uint64_t seed, double w1, double w2, double w3, double L,
+                                      int n, unsigned long long* mism) {
+  float wh[3], wl[3];
+  const double wd[3] = {w1, w2, w3};
+  for (int q = 0; q < 3; ++q) {
+    wh[q] = __double2float_rn(wd[q]);
+    wl[q] = __double2float_rn(wd[q] - (double)wh[q]);
+  }
+  unsigned long long ms = 0, mq = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const uint64_t h0 = sm64(seed ^ (uint64_t)i), h1 = sm64(h0), h2 = sm64(h1), h3 = sm64(h2), h4 = sm64(h3);
+    // order sum: potentials of three orders with decreasing magnitudes
+    const float a1 = unit_f(h0) * 1e3f, a2 = unit_f(h1) * 10.0f, a3 = unit_f(h2) * 0.1f;
+    float rh = 0.f, rl = 0.f;
+    mf::ff_axpy(wh[0], wl[0], a1, rh, rl);
+    mf::ff_axpy(wh[1], wl[1], a2, rh, rl);
+    mf::ff_axpy(wh[2], wl[2], a3, rh, rl);
+    const float ff = rh + rl;
+    const float dd = __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(w1, (double)a1), __dmul_rn(w2, (double)a2)),
+                                                 __dmul_rn(w3, (double)a3)));
+    ms += (ff != dd);
+    // q + Psi: q = (idx + s) / n * L with s in {0, 1/4, 1/2}, as a float pair
+    const int idx = (int)(h3 % (uint64_t)n);
+    const double s = 0.25 * (double)((h3 >> 32) % 3u);
+    const double q = __dmul_rn(__ddiv_rn((double)idx + s, (double)n), L);
+    const float qh = __double2float_rn(q);
+    const float2 qf = make_float2(qh, __double2float_rn(q - (double)qh));
+    const float psi = unit_f(h4) * 5.0f;
+    mq += (mf::ff_add_q(qf, psi) != __double2float_rn(__dadd_rn(q, (double)psi)));
+  }
+  if (ms) atomicAdd(&mism[0], ms);
+  if (mq) atomicAdd(&mism[1], mq);
+}
+}  // namespace
+
+extern "C" int mf_selftest_float_pairs(mf_ctx* c, long long count, uint64_t seed, double Dplus, long long* mism_sum,
+                                       long long* mism_q) {
+  if (!c || count < 1 || !mism_sum || !mism_q) return MF_ERR_ARG;
+  cudaSetDevice(c->device);
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return mf::set_err(c, MF_ERR_OOM, "mf_selftest_float_pairs");
+  cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), c->stream);
+  const double w1 = -Dplus, w2 = -3.0 / 7.0 * Dplus * Dplus, w3 = Dplus * Dplus * Dplus / 3.0;
+  k_float_pair_selftest<<<152 * 8, 256, 0, c->stream>>>(count, seed, w1, w2, w3, 1000.0, 512, d);
+  unsigned long long h[2] = {0, 0};
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return mf::cuda_err(c, e, "mf_selftest_float_pairs");
+  *mism_sum = (long long)h[0];
+  *mism_q = (long long)h[1];
+  return MF_OK;
+}
