@@ -482,6 +482,80 @@ def run_serve(args, device, prec, seconds):
             "peak_device_GB": round(st["peak_bytes"] / 1e9, 2), "pooled_pipelines": st["pooled_pipelines"]}
 
 
+def run_serve_replicas(args, job, device, prec, seconds):
+    """the same Poisson stream served by every rank's GPU from one shared
+    queue (replicas.ClaimQueue on the job's store): rank 0 pushes the
+    arrivals, each rank claims requests while fewer than 2 x workers of its own
+    are in flight and serves them with its own server; latencies are measured
+    from the push (one machine, one clock)"""
+    import json
+    import threading
+    import numpy as np
+    import torch.distributed as dist
+    from monofonic_gb300 import ic as _ic
+    from monofonic_gb300.replicas import ClaimQueue
+    from monofonic_gb300.serve import Server, Request
+    q = ClaimQueue(dist.distributed_c10d._get_default_store(), prefix=f"serve_{prec}")
+    srv = Server(nworkers=args.serve_workers, output="count", device=device)
+    for n in SERVE_SIZES:
+        for o in (2, 3):
+            srv.submit(Request(ngrid=n, boxlen=2.0 * n, zstart=WORKLOAD["zstart"], lpt_order=o, precision=prec))
+    srv.drain(600.0)
+    job.barrier()
+    feeder = None
+    if job.rank == 0:
+        rng = np.random.default_rng(7 if prec == "f32" else 8)
+
+        def feed():
+            start = time.time()
+            t_next = start
+            while t_next - start < seconds:
+                dt = t_next - time.time()
+                if dt > 0:
+                    time.sleep(dt)
+                r = _draw_request(rng, SERVE_SIZES, prec)
+                q.push(json.dumps({"n": r.ngrid, "o": r.lpt_order, "seed": r.seed, "t": time.time(),
+                                   "cos": [r.cosmology.Omega_m, r.cosmology.sigma_8, r.cosmology.n_s]}))
+                t_next += float(rng.exponential(1.0 / args.serve_rate))
+            q.close_input()
+        feeder = threading.Thread(target=feed)
+        feeder.start()
+    mine, lat, inflight = 0, [], {}
+
+    def reap():
+        for rid in list(inflight):
+            if srv.poll(rid) is not None:
+                lat.append((time.time() - inflight.pop(rid)) * 1e3)
+
+    while True:
+        while len(inflight) >= 2 * args.serve_workers:
+            reap()
+            time.sleep(0.0005)
+        c = q.claim(timeout_s=max(120.0, 4 * seconds))
+        if c is None:
+            break
+        d = json.loads(c[1])
+        cos = _ic.Cosmology(Omega_m=d["cos"][0], Omega_b=COSMO["Omega_b"], h=COSMO["h"], sigma_8=d["cos"][1],
+                            n_s=d["cos"][2])
+        rid = srv.submit(Request(ngrid=d["n"], boxlen=2.0 * d["n"], zstart=WORKLOAD["zstart"], lpt_order=d["o"],
+                                 lattice="sc", precision=prec, cosmology=cos, seed=d["seed"]))
+        inflight[rid] = d["t"]
+        mine += 1
+    while inflight:
+        reap()
+        time.sleep(0.0005)
+    if feeder is not None:
+        feeder.join()
+    srv.close()
+    total = job.sum_over_ranks(float(mine))
+    return {"precision": prec, "arrival_rate_per_s": args.serve_rate, "window_s": seconds, "requests": int(total),
+            "replicas": job.world, "served_by_rank0": mine,
+            "latency_ms": {"p50": job.max_over_ranks(_pct(lat, 0.5) if lat else 0.0),
+                           "p99": job.max_over_ranks(_pct(lat, 0.99) if lat else 0.0),
+                           "max": job.max_over_ranks(max(lat) if lat else 0.0)},
+            "requests_per_s": total / seconds, "capacity_req_per_s": None, "overloaded": None}
+
+
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
@@ -672,9 +746,10 @@ def run_mf(args):
         batch = run_batch(args, local)
     serving = None
     if not args.no_serve:
-        serving = {"f32": run_serve(args, local, "f32", args.serve_seconds)}
+        serve = run_serve if world == 1 else (lambda a, d, p, sec: run_serve_replicas(a, job, d, p, sec))
+        serving = {"f32": serve(args, local, "f32", args.serve_seconds)}
         if not args.no_fp64:
-            serving["f64"] = run_serve(args, local, "f64", args.serve_seconds_fp64)
+            serving["f64"] = serve(args, local, "f64", args.serve_seconds_fp64)
 
     if rank == 0:
         p50 = lat[len(lat) // 2]

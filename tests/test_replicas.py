@@ -78,3 +78,109 @@ def test_bench_gpus_2_starts_two_ranks():
     assert d["n_gpus"] == 2 and d["ranks_joined"] == 2
     # both ranks' units over the slowest rank's time
     assert d["value"] == pytest.approx(2 * 3000.0 / (d["ms_per_step"] * 3 / 1e3), rel=1e-9)
+
+
+# ---------------------------------------------------------------------------
+# replica serving over one shared queue (monofonic_gb300/replicas.py)
+# ---------------------------------------------------------------------------
+class _FakeServer:
+    """a device server without a device: each request takes cost / speed
+    seconds on a worker thread (the Server interface: submit / poll / close)"""
+
+    def __init__(self, device, speed):
+        import threading
+        self.device, self.speed = device, speed
+        self.done, self.next, self.lock = {}, 0, threading.Lock()
+        self.sem = threading.Semaphore(2)  # two requests overlap on a fake device
+
+    def submit(self, req):
+        import threading
+        import time
+        with self.lock:
+            rid = self.next
+            self.next += 1
+
+        def work():
+            with self.sem:
+                time.sleep(req["cost"] / self.speed)
+            with self.lock:
+                self.done[rid] = {"status": 0, "key": req["key"]}
+        threading.Thread(target=work, daemon=True).start()
+        return rid
+
+    def poll(self, rid):
+        with self.lock:
+            return self.done.get(rid)
+
+    def close(self):
+        pass
+
+
+def test_replica_server_shares_one_queue():
+    """two fake devices (one four times faster) pull from one FIFO queue:
+    every request finishes exactly once with its own result, requests leave
+    the queue in arrival order, and the faster device serves more of them"""
+    from monofonic_gb300.replicas import ReplicaServer
+    speeds = {0: 1.0, 1: 4.0}
+    rs = ReplicaServer([0, 1], lambda d: _FakeServer(d, speeds[d]), depth=2)
+    gids = [rs.submit({"cost": 0.01, "key": k}) for k in range(60)]
+    rs.drain(60.0)
+    res = [rs.wait(g, 10.0) for g in gids]
+    assert [r["key"] for r in res] == list(range(60))
+    assert rs.order == sorted(rs.order) and len(rs.order) == 60
+    per = rs.per_device()
+    assert sum(per.values()) == 60 and per[1] > per[0]
+    rs.close()
+
+
+def _claim_rank(rank, world, port, out_dir, nreq):
+    import json
+    import threading
+    import time
+    import torch.distributed as dist
+    from monofonic_gb300.replicas import ClaimQueue
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo")
+    store = dist.distributed_c10d._get_default_store()
+    q = ClaimQueue(store, prefix="t")
+    if rank == 0:  # the submitter: requests arrive while the replicas work
+        def feed():
+            for i in range(nreq):
+                q.push(json.dumps({"key": i}))
+                time.sleep(0.001)
+            q.close_input()
+        th = threading.Thread(target=feed)
+        th.start()
+    mine = []
+    per_req = 0.002 if rank == 0 else 0.008  # rank 1 is four times slower
+    while True:
+        c = q.claim(timeout_s=30.0)
+        if c is None:
+            break
+        idx, payload = c
+        time.sleep(per_req)
+        q.complete(idx, json.dumps({"key": json.loads(payload)["key"], "rank": rank}))
+        mine.append(idx)
+    if rank == 0:
+        th.join()
+    dist.barrier()
+    if rank == 0:
+        results = [json.loads(q.result(i)) for i in range(nreq)]
+        assert [r["key"] for r in results] == list(range(nreq)) and q.completed() == nreq
+    dist.barrier()
+    dist.destroy_process_group()
+    with open(os.path.join(out_dir, f"claims{rank}.json"), "w") as f:
+        json.dump(mine, f)
+
+
+def test_claim_queue_two_gloo_ranks(tmp_path):
+    """two ranks serve one queue that a third party keeps filling: every
+    request is claimed by exactly one rank, and the faster rank takes more"""
+    import json
+    import torch.multiprocessing as mp
+    nreq = 80
+    mp.spawn(_claim_rank, args=(2, _free_port(), str(tmp_path), nreq), nprocs=2, join=True)
+    c0 = json.loads((tmp_path / "claims0.json").read_text())
+    c1 = json.loads((tmp_path / "claims1.json").read_text())
+    assert sorted(c0 + c1) == list(range(nreq))
+    assert len(c0) > len(c1) > 0
