@@ -10,9 +10,12 @@ transfer function, seeded N(0,1) white noise (synthetic; no dataset).
           HBM when the timed region starts, particles (positions, velocities,
           IDs) resident in HBM when it ends; CUDA events on the pipeline's
           stream; the working set (>16 GB) is far larger than L2.
-  e2e     the same through the public C ABI (mf_ic_set_noise + mf_ic_run)
-          with the noise copied from page-locked host memory and all
-          particles copied back to page-locked host memory every step.
+  e2e     the same through the public C ABI (mf_ic_set_noise +
+          mf_ic_run_async, mf_ic_wait after the last step) with the noise
+          copied from page-locked host memory and all particles copied back
+          to page-locked host memory every step; a run's particle copies
+          overlap the next run's fields (sync_ms_per_step: one synchronous
+          mf_ic_run per step instead).
   fp64    the plain FP64 form on the same workload (positions in double).
 
 --impl reference times the reference's CPU path on the host cores: whole
@@ -26,6 +29,7 @@ collectives on the data path); value is the sum over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -672,43 +676,62 @@ def run_mf(args):
         pos = ic.PinnedBuffer(gen32.pos_bytes)
         vel = ic.PinnedBuffer(gen32.vel_bytes)
         ids = ic.PinnedBuffer(gen32.id_bytes)
-        for _ in range(max(1, args.warmup)):
-            gen32.set_noise_host_ptr(pin_noise.ptr)
-            gen32.run_into(pos.ptr, vel.ptr, ids.ptr)
-        barrier()
-        ctx.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        w0 = time.perf_counter()
-        e0.record(stream)
-        for _ in range(args.steps):
-            gen32.set_noise_host_ptr(pin_noise.ptr)
-            gen32.run_into(pos.ptr, vel.ptr, ids.ptr)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ctx.synchronize()
-        wall_ms = (time.perf_counter() - w0) * 1e3 / args.steps
-        t = max_over_ranks(e0.elapsed_time(e1))
-        # the part of the last step after its last kernel: the streamed
+        def e2e_steps(steps, queued):
+            """steps ICs, each with its noise uploaded from page-locked host
+            memory and its particles copied back into page-locked host
+            buffers.  queued: through mf_ic_run_async (a run's particle copies
+            overlap the next run's fields, the next noise upload overlaps the
+            run before it; mf_ic_wait ends the region after the last copy);
+            else one synchronous mf_ic_run per step"""
+            barrier()
+            ctx.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            w0 = time.perf_counter()
+            e0.record(stream)
+            for _ in range(steps):
+                gen32.set_noise_host_ptr(pin_noise.ptr)
+                if queued:
+                    gen32.run_into_async(pos.ptr, vel.ptr, ids.ptr)
+                else:
+                    gen32.run_into(pos.ptr, vel.ptr, ids.ptr)
+            gen32.wait()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ctx.synchronize()
+            return max_over_ranks(e0.elapsed_time(e1)), (time.perf_counter() - w0) * 1e3 / steps
+
+        e2e_steps(max(1, args.warmup), True)
+        t, wall_ms = e2e_steps(args.steps, True)
+        # the part of the last step after its last kernel: its streamed
         # particle copies still in flight (the copy engine runs at the box's
         # pinned-copy rate; the slices become final only in the assembly)
         handoff_tail_ms = gen32.stage_times()[7]
+        t_sync, _ = e2e_steps(args.steps, False)
         ids_h = ids.array(np.uint64, (npart,))
         assert ids_h[1] == 2 and ids_h[n ** 3] == 1, "particle IDs wrong after e2e run"
         # the box's raw device-to-host copy rate into page-locked memory, for context
+        # (five samples: on shared hosts the link's rate into page-locked
+        # memory varies from copy to copy)
         probe = torch.empty(1 << 30, dtype=torch.uint8, device=torch.device("cuda", local))
-        best = 1e30
-        for _ in range(3):
+        rates = []
+        for _ in range(5):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             mf.lib().mf_copy_to_host(pos.ptr, probe.data_ptr(), probe.numel())
-            best = min(best, time.perf_counter() - t0)
+            rates.append(round((1 << 30) / (time.perf_counter() - t0) / 1e9, 1))
         del probe
+        hp = C.c_size_t()
+        mf.lib().mf_host_huge_page_bytes(C.byref(hp))
         e2e = {"value": world * npart * args.steps / (t / 1e3), "unit": UNIT,
                "h2d_bytes_per_step": int(noise_h.nbytes),
                "d2h_bytes_per_step": int(gen32.pos_bytes + gen32.vel_bytes + gen32.id_bytes),
                "ms_per_step": t / args.steps, "wall_ms_per_step": wall_ms,
-               "box_d2h_GBps_pinned_1GiB": round((1 << 30) / best / 1e9, 1),
+               "api": "mf_ic_set_noise (host) + mf_ic_run_async per step, mf_ic_wait at the end",
+               "sync_ms_per_step": round(t_sync / args.steps, 3),
+               "box_d2h_GBps_pinned_1GiB": max(rates), "box_d2h_GBps_samples": rates,
+               "host_buffers": (f"mf_host_alloc: {hp.value >> 20} MB transparent huge pages, registered"
+                                if hp.value else "mf_host_alloc: cudaHostAlloc"),
                "handoff_tail_ms_last_step": round(handoff_tail_ms, 2)}
         for b in (pin_noise, pos, vel, ids):
             b.close()

@@ -81,9 +81,15 @@ int mf_ctx_profile_read(mf_ctx* ctx, double* ms, int64_t* counts, int n);
  * MF_PREC_F32), the arithmetic ceiling of the FP64 path's roofline (no
  * reference counterpart) */
 int mf_probe_fma_rate(mf_ctx* ctx, int prec, double* tflops);
-/* page-locked host memory for streaming transfers (no reference counterpart) */
+/* page-locked host memory for streaming transfers (no reference
+ * counterpart).  A buffer of at least one transparent huge page is backed by
+ * huge pages (rounded up to whole pages) and registered with the driver,
+ * which keeps copies over the host link at their full rate; smaller buffers
+ * come from cudaHostAlloc.  Free with mf_host_free only. */
 int mf_host_alloc(size_t bytes, void** out);
 int mf_host_free(void* p);
+/* the huge page size mf_host_alloc backs large buffers with (0: none) */
+int mf_host_huge_page_bytes(size_t* bytes);
 /* synchronous copy of device memory (e.g. particles of mf_ic_particles) to
  * host memory (no reference counterpart) */
 int mf_copy_to_host(void* host, const void* device, size_t bytes);

@@ -148,6 +148,19 @@ int mf_ic_set_cosmology(mf_ic* ic, const mf_cosmo_scalars* cosmo);
  * buffers of the ic when out->location is MF_LOC_DEVICE and out->pos is
  * NULL; copies to host buffers when MF_LOC_HOST); synchronous */
 int mf_ic_run(mf_ic* ic, mf_particles* out);
+/* mf_ic_run into host buffers (out->location MF_LOC_HOST), returning without
+ * waiting.  The particles are copied on the pipeline's copy stream as they
+ * become final; the context's stream does not wait for those copies, so the
+ * next run queued on the pipeline computes its fields while this run's
+ * particles are still crossing to the host (the next run writes its particle
+ * buffers only after them).  A host noise upload (mf_ic_set_noise) queued
+ * after this call likewise overlaps this run.  The host buffers are complete,
+ * and the host noise buffers of the queued runs may be reused, once
+ * mf_ic_wait (or a synchronous run) returns.  Device errors of the queued
+ * runs are reported there. */
+int mf_ic_run_async(mf_ic* ic, const mf_particles* out);
+/* wait for every queued run of the pipeline, its host copies included */
+int mf_ic_wait(mf_ic* ic);
 /* enqueue the same pipeline on the context's stream and return without
  * waiting; the particles stay in the ic's device buffers (mf_ic_particles).
  * While the stream is being captured into a CUDA graph the work is recorded

@@ -41,6 +41,7 @@ SIGNATURES = {
                                           C.POINTER(C.c_longlong)]),
     "mf_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "mf_host_free": (C.c_int, [C.c_void_p]),
+    "mf_host_huge_page_bytes": (C.c_int, [C.POINTER(C.c_size_t)]),
     "mf_grid_size_supported": (C.c_int, [C.c_int]),
     "mf_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "mf_ctx_destroy": (C.c_int, [C.c_void_p]),
@@ -118,6 +119,8 @@ SIGNATURES.update({
     "mf_ic_destroy": (C.c_int, [C.c_void_p]),
     "mf_ic_set_noise": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "mf_ic_run": (C.c_int, [C.c_void_p, C.POINTER(mf_particles)]),
+    "mf_ic_run_async": (C.c_int, [C.c_void_p, C.POINTER(mf_particles)]),
+    "mf_ic_wait": (C.c_int, [C.c_void_p]),
     "mf_ic_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "mf_ic_get_potential": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "mf_ic_get_noise": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),

@@ -1,9 +1,14 @@
 // C ABI of libmfgpu: context, Grid_FFT and convolver handles.
+#include <sys/mman.h>
+
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "mf_runtime.h"
@@ -757,6 +762,8 @@ extern "C" int mf_ctx_profile_read(mf_ctx* c, double* ms, int64_t* counts, int n
     if (cudaEventElapsedTime(&t, rec.second.first, rec.second.second) == cudaSuccess && rec.first < n) {
       ms[rec.first] += t;
       counts[rec.first] += 1;
+    } else {
+      cudaGetLastError();  // an unrecorded pair is skipped, not left for the next call to report
     }
     c->event_pool.push_back(rec.second.first);
     c->event_pool.push_back(rec.second.second);
@@ -765,15 +772,102 @@ extern "C" int mf_ctx_profile_read(mf_ctx* c, double* ms, int64_t* counts, int n
   return MF_OK;
 }
 
+// ---------------------------------------------------------------------------
+// page-locked host buffers.  A buffer of at least one transparent huge page
+// is an anonymous private mapping aligned to the kernel's PMD page size,
+// advised MADV_HUGEPAGE, first-touched and then registered with the driver:
+// the device reaches it through a few large translations.  On the GB300 host
+// link, buffers of base pages (cudaHostAlloc, or malloc + cudaHostRegister)
+// had whole copies drop from 193 GB/s (device to host) and 211 GB/s (host to
+// device) to 12-60 GB/s at irregular times, while huge-page buffers kept the
+// full rate.  Smaller buffers, and hosts without transparent huge pages, use
+// cudaHostAlloc.
+// ---------------------------------------------------------------------------
+namespace {
+struct HostMapping {
+  void* base;
+  size_t len;
+};
+std::mutex g_host_mu;
+std::unordered_map<void*, HostMapping> g_host_maps;
+
+// PMD huge page size when transparent huge pages can be requested, else 0
+size_t thp_bytes() {
+  static const size_t sz = [] {
+    unsigned long long v = 0;
+    if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+      if (std::fscanf(f, "%llu", &v) != 1) v = 0;
+      std::fclose(f);
+    }
+    char mode[128] = {0};
+    if (FILE* f = std::fopen("/sys/kernel/mm/transparent_hugepage/enabled", "r")) {
+      if (!std::fgets(mode, sizeof mode, f)) mode[0] = 0;
+      std::fclose(f);
+    }
+    if (!std::strstr(mode, "[always]") && !std::strstr(mode, "[madvise]")) v = 0;
+    return (size_t)v;
+  }();
+  return sz;
+}
+
+void* thp_alloc(size_t bytes) {
+  const size_t hp = thp_bytes();
+  if (!hp || bytes < hp) return nullptr;
+  const size_t len = (bytes + hp - 1) / hp * hp;
+  char* raw = (char*)mmap(nullptr, len + hp, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (raw == MAP_FAILED) return nullptr;
+  char* a = (char*)(((uintptr_t)raw + hp - 1) / hp * hp);
+  if (a > raw) munmap(raw, (size_t)(a - raw));  // trim the alignment slack
+  if (a + len < raw + len + hp) munmap(a + len, (size_t)(raw + len + hp - (a + len)));
+  madvise(a, len, MADV_HUGEPAGE);
+  madvise(a, len, MADV_DONTFORK);  // a child process must not share the registered pages copy-on-write
+  std::memset(a, 0, len);          // first touch: faulted in as huge pages
+  if (cudaHostRegister(a, len, cudaHostRegisterPortable) != cudaSuccess) {
+    cudaGetLastError();
+    munmap(a, len);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_maps[a] = HostMapping{a, len};
+  return a;
+}
+}  // namespace
+
 extern "C" int mf_host_alloc(size_t bytes, void** out) {
   if (!out) return MF_ERR_ARG;
-  *out = nullptr;
-  if (cudaHostAlloc(out, bytes, cudaHostAllocPortable) != cudaSuccess) return MF_ERR_OOM;
+  *out = thp_alloc(bytes);
+  if (*out) return MF_OK;
+  if (cudaHostAlloc(out, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return MF_ERR_OOM;
+  }
   return MF_OK;
 }
 
 extern "C" int mf_host_free(void* p) {
-  if (p) cudaFreeHost(p);
+  if (!p) return MF_OK;
+  HostMapping m{nullptr, 0};
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_maps.find(p);
+    if (it != g_host_maps.end()) {
+      m = it->second;
+      g_host_maps.erase(it);
+    }
+  }
+  if (m.base) {
+    cudaHostUnregister(m.base);
+    munmap(m.base, m.len);
+  } else {
+    cudaFreeHost(p);
+  }
+  return MF_OK;
+}
+
+extern "C" int mf_host_huge_page_bytes(size_t* bytes) {
+  if (!bytes) return MF_ERR_ARG;
+  *bytes = thp_bytes();
   return MF_OK;
 }
 

@@ -373,10 +373,19 @@ struct mf_ic {
   bool has_tk = false;      // amp + nk2 holds a tabulated T(k)
   ICDyn* dyn_h = nullptr;   // page-locked host copy, copied to dyn_d at the start of each run
   ICDyn* dyn_d = nullptr;
-  // host hand-off: the positions are copied on a second stream while the
-  // velocities are being assembled
+  // host hand-off: the particles are copied on a second stream while the
+  // rest of the run computes.  ev_copy follows the last copy queued on it,
+  // ev_ids the last copy of the IDs; a run waits for them before it writes
+  // the particle buffers again, so an asynchronous run's copies overlap the
+  // next run's fields
   cudaStream_t cstream = nullptr;
-  cudaEvent_t ev_pos = nullptr, ev_copy = nullptr;
+  cudaEvent_t ev_pos = nullptr, ev_copy = nullptr, ev_ids = nullptr;
+  mf_particles early_out{};  // host destinations of the run being enqueued asynchronously
+  // host noise uploads of an FP32 pipeline: copied into the staging buffer on
+  // their own stream once the previous upload has been converted, so that an
+  // upload overlaps the run before it
+  cudaStream_t hstream = nullptr;
+  cudaEvent_t ev_stage_free = nullptr, ev_stage_full = nullptr;
   const mf_particles* early = nullptr;
   bool early_all = false;  // every particle array was streamed to the host during the run
   bool pos_early = false;  // the positions were copied during the run
@@ -722,6 +731,8 @@ int enqueue_impl(mf_ic* ic) {
   // ---- particle IDs (particle_generator.hh:212-253): independent of the
   // fields, so they are made first and their copy overlaps the whole run
   if (!fields) {
+    // (after the previous run's copy of them, which may still be queued)
+    if (!c->capturing && ic->ev_ids) CK(cudaStreamWaitEvent(s, ic->ev_ids, 0));
     LaunchScope ls(c, KK_POINTWISE);
     if (p.id64)
       k_ids<uint64_t><<<blocks_for((size_t)n * n * n), kThreads, 0, s>>>((uint64_t*)ic->dids, n, overload, 0);
@@ -730,6 +741,7 @@ int enqueue_impl(mf_ic* ic) {
     CK(cudaGetLastError());
     if (ic->early) {  // the IDs' copy overlaps the whole run
       CK(early_copy(ic->early->ids, ic->dids, ic->id_bytes));
+      CK(cudaEventRecord(ic->ev_ids, ic->cstream));
       ic->ids_early = true;
     }
     if (p.baryons) {  // baryon IDs start at IDoffset = 1 (ic_generator.cc:626-628)
@@ -866,6 +878,9 @@ int enqueue_impl(mf_ic* ic) {
   // species of the Lagrangian assembly: dark matter, then the baryons on the
   // secondary lattice; with field output the baryons take the Eulerian branch
   const int nsp = (p.baryons && !fields) ? 2 : 1;
+  // the particle buffers are rewritten below: after every copy of them that
+  // an earlier asynchronous run queued on the copy stream
+  if (!c->capturing && ic->ev_copy) CK(cudaStreamWaitEvent(s, ic->ev_copy, 0));
   for (int pass = 0; pass < 2; ++pass) {  // 0: positions, 1: velocities
     const bool vel = pass == 1;
     for (int sp = 0; sp < nsp; ++sp) {
@@ -1057,8 +1072,10 @@ int enqueue_impl(mf_ic* ic) {
   return MF_OK;
 }
 
-// hand-off of the particles (device pointers, or copies into host buffers)
-int handoff(mf_ic* ic, mf_particles* out) {
+// hand-off of the particles (device pointers, or copies into host buffers).
+// Asynchronous (host buffers only): the copies not streamed during the run go
+// on the copy stream too, and the context's stream does not wait for them
+int handoff(mf_ic* ic, mf_particles* out, bool async) {
   mf_ctx* c = ic->ctx;
   cudaStream_t s = c->stream;
   const bool fields = ic->p.out_kind == MF_OUT_FIELDS;
@@ -1072,6 +1089,22 @@ int handoff(mf_ic* ic, mf_particles* out) {
     out->npart = ic->npart;
     if (out->location == MF_LOC_HOST) {
       if (!out->pos || !out->vel || (!fields && !out->ids)) return set_err(c, MF_ERR_ARG, "mf_ic_run: null host buffer");
+      if (async) {
+        cudaStream_t cs = ic->cstream;
+        if (!ic->early_all) {
+          CK(cudaEventRecord(ic->ev_pos, s));
+          CK(cudaStreamWaitEvent(cs, ic->ev_pos, 0));
+          if (!ic->pos_early) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, cs));
+          CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, cs));
+          if (!fields && !ic->ids_early) {
+            CK(cudaMemcpyAsync(out->ids, ic->dids, ic->id_bytes, cudaMemcpyDeviceToHost, cs));
+            CK(cudaEventRecord(ic->ev_ids, cs));
+          }
+          CK(cudaEventRecord(ic->ev_copy, cs));
+        }
+        CK(cudaEventRecord(ic->ev[8], cs));  // the end of the run's last copy
+        return MF_OK;
+      }
       if (!ic->early_all) {
         if (!ic->pos_early) CK(cudaMemcpyAsync(out->pos, ic->dpos, ic->pos_bytes, cudaMemcpyDeviceToHost, s));
         CK(cudaMemcpyAsync(out->vel, ic->dvel, ic->vel_bytes, cudaMemcpyDeviceToHost, s));
@@ -1146,6 +1179,8 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
   mf_ctx* c = ic->ctx;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (ic->cstream) cudaStreamSynchronize(ic->cstream);  // copies of an asynchronous run
+  if (ic->hstream) cudaStreamSynchronize(ic->hstream);  // a host noise upload
   if (ic->wn) mf_grid_destroy(ic->wn);
   for (auto& g : ic->f)
     if (g) mf_grid_destroy(g);
@@ -1178,12 +1213,10 @@ extern "C" int mf_ic_destroy(mf_ic* ic) {
     if (e) cudaEventDestroy(e);
   cudaFree(ic->dyn_d);
   cudaFreeHost(ic->dyn_h);
-  if (ic->cstream) {
-    cudaStreamSynchronize(ic->cstream);
-    cudaStreamDestroy(ic->cstream);
-  }
-  if (ic->ev_pos) cudaEventDestroy(ic->ev_pos);
-  if (ic->ev_copy) cudaEventDestroy(ic->ev_copy);
+  if (ic->cstream) cudaStreamDestroy(ic->cstream);
+  if (ic->hstream) cudaStreamDestroy(ic->hstream);
+  for (cudaEvent_t ev : {ic->ev_pos, ic->ev_copy, ic->ev_ids, ic->ev_stage_free, ic->ev_stage_full})
+    if (ev) cudaEventDestroy(ev);
   --c->children;
   delete ic;
   return MF_OK;
@@ -1394,11 +1427,25 @@ extern "C" int mf_ic_set_noise(mf_ic* ic, const double* noise, int location) {
     e = cudaMemcpy2DAsync(ic->wn->d, (size_t)(n + 2) * sizeof(double), noise, (size_t)n * sizeof(double),
                           (size_t)n * sizeof(double), (size_t)n * n, cudaMemcpyHostToDevice, c->stream);
   } else if (location == MF_LOC_HOST) {
-    // FP32 grid: through a staging buffer kept by the pipeline (allocated at the first host upload)
+    // FP32 grid: through a staging buffer kept by the pipeline (allocated at
+    // the first host upload).  The copy runs on the upload stream as soon as
+    // the previous upload has been converted, i.e. while the runs queued
+    // before it compute; the conversion into the grid is stream-ordered
     if (!ic->stage && (e = cudaMalloc((void**)&ic->stage, n3 * sizeof(double))) != cudaSuccess)
       return cuda_err(c, e, "mf_ic_set_noise: staging buffer");
-    e = cudaMemcpyAsync(ic->stage, noise, n3 * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (!ic->hstream) {
+      e = cudaStreamCreateWithFlags(&ic->hstream, cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ic->ev_stage_free, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ic->ev_stage_full, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_err(c, e, "mf_ic_set_noise: upload stream");
+      e = cudaEventRecord(ic->ev_stage_free, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ic->hstream, ic->ev_stage_free, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ic->stage, noise, n3 * sizeof(double), cudaMemcpyHostToDevice, ic->hstream);
+    if (e == cudaSuccess) e = cudaEventRecord(ic->ev_stage_full, ic->hstream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, ic->ev_stage_full, 0);
     if (e == cudaSuccess) e = pw_fill_from_f64<float>((float*)ic->wn->d, ic->stage, n, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ic->ev_stage_free, c->stream);
   } else {
     e = (ic->p.precision == MF_PREC_F64) ? pw_fill_from_f64<double>((double*)ic->wn->d, noise, n, c->stream)
                                          : pw_fill_from_f64<float>((float*)ic->wn->d, noise, n, c->stream);
@@ -1446,32 +1493,79 @@ extern "C" int mf_ic_enqueue(mf_ic* ic) {
   return rc;
 }
 
+namespace {
+void reset_early(mf_ic* ic) {
+  ic->early = nullptr;
+  ic->early_all = false;
+  ic->pos_early = false;
+  ic->ids_early = false;
+}
+
+// the copy stream and its events, created at the first host hand-off
+int make_copy_stream(mf_ic* ic, const char* where) {
+  cudaError_t e = cudaSuccess;
+  if (!ic->cstream) e = cudaStreamCreateWithFlags(&ic->cstream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !ic->ev_pos) e = cudaEventCreateWithFlags(&ic->ev_pos, cudaEventDisableTiming);
+  if (e == cudaSuccess && !ic->ev_copy) e = cudaEventCreateWithFlags(&ic->ev_copy, cudaEventDisableTiming);
+  if (e == cudaSuccess && !ic->ev_ids) e = cudaEventCreateWithFlags(&ic->ev_ids, cudaEventDisableTiming);
+  return e == cudaSuccess ? MF_OK : cuda_err(ic->ctx, e, where);
+}
+
+bool host_buffers(const mf_ic* ic, const mf_particles* out) {
+  return out && out->location == MF_LOC_HOST && out->pos && out->vel &&
+         (ic->p.out_kind == MF_OUT_FIELDS || out->ids);
+}
+}  // namespace
+
 extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic) return MF_ERR_ARG;
   if (ic->p.baryons) return set_err(ic->ctx, MF_ERR_ARG, "mf_ic_run: a two-species pipeline runs with mf_ic_run_species");
   if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
-  ic->early = nullptr;
-  ic->early_all = false;
-  ic->pos_early = false;
-  ic->ids_early = false;
-  if (out && out->location == MF_LOC_HOST && out->pos && out->vel &&
-      (ic->p.out_kind == MF_OUT_FIELDS || out->ids)) {
-    cudaError_t e = cudaSuccess;
-    if (!ic->cstream) e = cudaStreamCreateWithFlags(&ic->cstream, cudaStreamNonBlocking);
-    if (e == cudaSuccess && !ic->ev_pos) e = cudaEventCreateWithFlags(&ic->ev_pos, cudaEventDisableTiming);
-    if (e == cudaSuccess && !ic->ev_copy) e = cudaEventCreateWithFlags(&ic->ev_copy, cudaEventDisableTiming);
-    if (e != cudaSuccess) return cuda_err(ic->ctx, e, "mf_ic_run: copy stream");
+  reset_early(ic);
+  if (host_buffers(ic, out)) {
+    const int rc = make_copy_stream(ic, "mf_ic_run: copy stream");
+    if (rc != MF_OK) return rc;
     ic->early = out;
   }
   int rc = mf_ic_enqueue(ic);
-  if (rc == MF_OK) rc = handoff(ic, out);
+  if (rc == MF_OK) rc = handoff(ic, out, false);
   if (rc == MF_OK) rc = check_device_error(ic->ctx);
   else cudaStreamSynchronize(ic->ctx->stream);
   if (ic->cstream) cudaStreamSynchronize(ic->cstream);
-  ic->early = nullptr;
-  ic->early_all = false;
-  ic->pos_early = false;
-  ic->ids_early = false;
+  reset_early(ic);
+  return rc;
+}
+
+extern "C" int mf_ic_run_async(mf_ic* ic, const mf_particles* out) {
+  if (!ic) return MF_ERR_ARG;
+  mf_ctx* c = ic->ctx;
+  if (ic->p.baryons) return set_err(c, MF_ERR_ARG, "mf_ic_run_async: a two-species pipeline runs with mf_ic_run_species");
+  if (!host_buffers(ic, out)) return set_err(c, MF_ERR_ARG, "mf_ic_run_async: host buffers expected");
+  if (!ic->noise_set && !ic->noise_seeded) return set_err(c, MF_ERR_STATE, "mf_ic_run_async: white noise not set");
+  int rc = make_copy_stream(ic, "mf_ic_run_async: copy stream");
+  if (rc != MF_OK) return rc;
+  reset_early(ic);
+  ic->early_out = *out;
+  ic->early = &ic->early_out;
+  rc = mf_ic_enqueue(ic);
+  if (rc == MF_OK) rc = handoff(ic, &ic->early_out, true);
+  reset_early(ic);
+  if (rc != MF_OK) {  // nothing of a failed run stays in flight
+    cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(ic->cstream);
+  }
+  return rc;
+}
+
+extern "C" int mf_ic_wait(mf_ic* ic) {
+  if (!ic) return MF_ERR_ARG;
+  mf_ctx* c = ic->ctx;
+  cudaSetDevice(c->device);
+  int rc = check_device_error(c);
+  if (ic->cstream) {
+    const cudaError_t e = cudaStreamSynchronize(ic->cstream);
+    if (rc == MF_OK && e != cudaSuccess) rc = cuda_err(c, e, "mf_ic_wait: copy stream");
+  }
   return rc;
 }
 
@@ -1569,7 +1663,10 @@ extern "C" int mf_ic_stage_times(const mf_ic* ic, double* ms) {
   if (!ic || !ms) return MF_ERR_ARG;
   for (int i = 0; i < 8; ++i) {
     float t = 0;
-    if (cudaEventElapsedTime(&t, ic->ev[i], ic->ev[i + 1]) != cudaSuccess) t = -1;
+    if (cudaEventElapsedTime(&t, ic->ev[i], ic->ev[i + 1]) != cudaSuccess) {
+      t = -1;             // a stage the last run did not record
+      cudaGetLastError();  // (not an error of the next call's)
+    }
     ms[i] = t;
   }
   return MF_OK;

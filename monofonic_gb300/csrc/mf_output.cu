@@ -202,6 +202,7 @@ int write_component(mf_grafic2* w, const void* dfield, int prec, size_t row_stri
     if (e != cudaSuccess) break;
     float t = 0;
     if (cudaEventElapsedTime(&t, w->k0[b], w->k1[b]) == cudaSuccess) *kernel_ms += t;
+    else cudaGetLastError();  // timing only: not an error of a later call
     ok = write_all(fd, w->hbuf[b], (size_t)nz * rec * 4);
     bytes += (size_t)nz * rec * 4;
     if (ok && ch + 2 < nch) e = issue(ch + 2);

@@ -165,6 +165,20 @@ class ICGenerator:
         out.location = L.MF_LOC_HOST
         _check(self.ctx.ptr, lib().mf_ic_run(self.ptr, C.byref(out)))
 
+    def run_into_async(self, pos_ptr: int, vel_ptr: int, ids_ptr: int):
+        """queue a run whose particles are copied into caller-owned host
+        buffers (page-locked for overlap) and return at once; the buffers are
+        complete after wait().  The next queued run computes while this one's
+        particles are still being copied."""
+        out = L.mf_particles()
+        out.pos, out.vel, out.ids = pos_ptr, vel_ptr, ids_ptr
+        out.location = L.MF_LOC_HOST
+        _check(self.ctx.ptr, lib().mf_ic_run_async(self.ptr, C.byref(out)))
+
+    def wait(self):
+        """wait for every queued run, host copies included"""
+        _check(self.ctx.ptr, lib().mf_ic_wait(self.ptr))
+
     def run(self, to_host: bool = True):
         """Run the pipeline; returns (pos, vel, ids) numpy arrays, or device
         pointers when to_host is False."""
