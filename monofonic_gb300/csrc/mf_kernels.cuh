@@ -239,12 +239,12 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 // strided forward transform, truncation and inverse transform of one column in
 // one pass (ConvXTruncOp), persistent and double-buffered as k_colfft_pipe
 // ---------------------------------------------------------------------------
-template <typename T, int L, int NCOL>
+template <typename T, int L, int NCOL, class OP>
 __global__ void __launch_bounds__(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
                                   col_minb(NCOL * LineFFT<T, L, false, MF_COL_MAXR>::TPL,
                                            LineFFT<T, L, false, MF_COL_MAXR>::E, (int)sizeof(T)))
-k_colfft_trunc(ConvXTruncOp<T> op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
-  constexpr int LAY = col_layout<T, NCOL, ConvXTruncOp<T>>();
+k_colfft_trunc(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab) {
+  constexpr int LAY = col_layout<T, NCOL, OP>();
   using FF = LineFFT<T, L, false, MF_COL_MAXR, LAY>;
   using FI = LineFFT<T, L, true, MF_COL_MAXR, LAY>;
   static_assert(FF::E == FI::E && FF::TPL == FI::TPL, "one plan for both directions");

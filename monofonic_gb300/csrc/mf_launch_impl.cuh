@@ -112,6 +112,34 @@ cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, c
   }
 }
 
+// N-grid lengths, and the convolution pass lengths that have a compile-time
+// geometry: Orszag M = 3N/2 and aliased M = N for an N-grid length N
+__host__ __device__ constexpr bool ngrid_len(int L) {
+  return L == 16 || L == 32 || L == 64 || L == 96 || L == 128 || L == 192 || L == 256 || L == 384 || L == 512;
+}
+__host__ __device__ constexpr bool orszag_len(int L) { return L % 3 == 0 && ngrid_len(2 * L / 3); }
+
+// a convolution pass of length L (the padded axis, M = L) launched with its
+// geometry as compile-time constants; a geometry that is neither the Orszag
+// nor the aliased form of a compiled length is refused
+template <typename T, int L, class LAUNCH, class OP>
+cudaError_t with_conv_geom(const OP& op, LAUNCH&& go) {
+  if (op.g.orszag) {
+    if constexpr (orszag_len(L)) {
+      using G = CGeom<L, true>;
+      if (!geom_matches<G>(op.g)) return cudaErrorInvalidValue;
+      return go(op.template with_geom<G>());
+    }
+    return cudaErrorInvalidValue;
+  }
+  if constexpr (ngrid_len(L)) {
+    using G = CGeom<L, false>;
+    if (!geom_matches<G>(op.g)) return cudaErrorInvalidValue;
+    return go(op.template with_geom<G>());
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <typename T, int H, class OP>
 cudaError_t launch_zr2c(OP op, int nlines, int kout, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
   constexpr int LPB = z_lpb<T, H, H + 1>();
@@ -339,23 +367,27 @@ template cudaError_t Launch<MF_T>::z_c2r_plain(int, PlainZOp<MF_T>, int, int, co
 template <typename T>
 cudaError_t Launch<T>::conv_xinv(int L, ConvXInvOp<T> op, int nslab, int ncols, int nops,
                                  const cplx<T>* tw, cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s, KK_CONV_XINV);
+#define CASE(LL)                                                                                        \
+  case LL:                                                                                             \
+    return with_conv_geom<T, LL>(op, [&](auto o) { return launch_col<T, LL, true>(o, nslab, ncols, nops, tw, s, KK_CONV_XINV); });
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
 template <typename T>
 cudaError_t Launch<T>::conv_xfwd(int L, ConvXFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                  cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_CONV_XFWD);
+#define CASE(LL)                                                                                        \
+  case LL:                                                                                             \
+    return with_conv_geom<T, LL>(op, [&](auto o) { return launch_col<T, LL, false>(o, nslab, ncols, 1, tw, s, KK_CONV_XFWD); });
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
-template <typename T, int L>
-cudaError_t launch_xtrunc(ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T>* tw, cudaStream_t s) {
+template <typename T, int L, class OP>
+cudaError_t launch_xtrunc(OP op, int nslab, int ncols, const cplx<T>* tw, cudaStream_t s) {
   constexpr int NC = pipe_ncol<T, L>();
   constexpr int TPL = LineFFT<T, L, false, MF_COL_MAXR>::TPL;
   const size_t smem = (size_t)2 * L * NC * sizeof(cplx<T>);
-  auto kern = k_colfft_trunc<T, L, NC>;
+  auto kern = k_colfft_trunc<T, L, NC, OP>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0, nsm = 0, dev = 0;
@@ -374,7 +406,9 @@ cudaError_t launch_xtrunc(ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T
 template <typename T>
 cudaError_t Launch<T>::conv_xtrunc(int L, ConvXTruncOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                    cudaStream_t s) {
-#define CASE(LL) case LL: return launch_xtrunc<T, LL>(op, nslab, ncols, tw, s);
+#define CASE(LL)                                                                                        \
+  case LL:                                                                                             \
+    return with_conv_geom<T, LL>(op, [&](auto o) { return launch_xtrunc<T, LL>(o, nslab, ncols, tw, s); });
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
@@ -387,14 +421,18 @@ template cudaError_t Launch<MF_T>::conv_xtrunc(int, ConvXTruncOp<MF_T>, int, int
 template <typename T>
 cudaError_t Launch<T>::conv_yinv(int L, ConvYInvOp<T> op, int nslab, int ncols, int nops,
                                  const cplx<T>* tw, cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, true>(op, nslab, ncols, nops, tw, s, KK_CONV_YINV);
+#define CASE(LL)                                                                                        \
+  case LL:                                                                                             \
+    return with_conv_geom<T, LL>(op, [&](auto o) { return launch_col<T, LL, true>(o, nslab, ncols, nops, tw, s, KK_CONV_YINV); });
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
 template <typename T>
 cudaError_t Launch<T>::conv_yfwd(int L, ConvYFwdOp<T> op, int nslab, int ncols, const cplx<T>* tw,
                                  cudaStream_t s) {
-#define CASE(LL) case LL: return launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_CONV_YFWD);
+#define CASE(LL)                                                                                        \
+  case LL:                                                                                             \
+    return with_conv_geom<T, LL>(op, [&](auto o) { return launch_col<T, LL, false>(o, nslab, ncols, 1, tw, s, KK_CONV_YFWD); });
   switch (L) { MF_LEN_CONV(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
