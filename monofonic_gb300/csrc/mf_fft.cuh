@@ -31,11 +31,39 @@ template <typename C>
 __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename C>
 __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// complex products with one fused multiply-add per component (the build
+// compiles with FP contraction off, which the float-pair arithmetic below
+// needs; here the fusion is explicit)
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+#ifndef MF_FFT_FMA
+#define MF_FFT_FMA 1
+#endif
 template <typename C>
-__device__ __forceinline__ C cmul(C a, C b) { C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r; }
+__device__ __forceinline__ C cmul(C a, C b) {
+  C r;
+  if (MF_FFT_FMA) {
+    r.x = fma_rn(a.x, b.x, -(a.y * b.y));
+    r.y = fma_rn(a.x, b.y, a.y * b.x);
+  } else {
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+  }
+  return r;
+}
 // a * conj(b)
 template <typename C>
-__device__ __forceinline__ C cmulc(C a, C b) { C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r; }
+__device__ __forceinline__ C cmulc(C a, C b) {
+  C r;
+  if (MF_FFT_FMA) {
+    r.x = fma_rn(a.x, b.x, a.y * b.y);
+    r.y = fma_rn(a.y, b.x, -(a.x * b.y));
+  } else {
+    r.x = a.x * b.x + a.y * b.y;
+    r.y = a.y * b.x - a.x * b.y;
+  }
+  return r;
+}
 template <typename C, typename T>
 __device__ __forceinline__ C cscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
 template <typename C>
