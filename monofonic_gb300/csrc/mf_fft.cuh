@@ -326,6 +326,7 @@ template <typename T, int L, bool INV, int MAXR = 8, int LAYOUT = 0, bool HOIST 
 struct LineFFT {
   static_assert(plan_ok(L), "FFT length must be 2^a 3^b >= 4");
   using C = cplx<T>;
+  static constexpr int LEN = L;
   static constexpr int NS = plan_nstages(L, MAXR);
   static constexpr int E = plan_elems(L, MAXR);
   static constexpr int TPL = L / E;

@@ -625,6 +625,33 @@ __device__ __forceinline__ cplx<T> c2r_pre_s(const cplx<T>* src, int k, int kin,
   return mkc<T>(Ev.x - Ov.y, Ev.y + Ov.x);
 }
 
+// Output slots of a line FFT held as k = t + TPL a(s): the r2c post-processing
+// pairs Z[k] with Z[H - k], which then sits in lane (TPL - t) mod TPL of the
+// same line group, slot a' = E - 1 - a (or (E - a) mod E in lane 0), so one
+// warp shuffle per slot replaces a shared-memory round trip.
+template <class F>
+__host__ __device__ constexpr int zslot_a(int s) {
+  return s / F::RL + (F::TPL > 0 ? (F::LEN / F::RL) / F::TPL : 0) * (s % F::RL);
+}
+template <class F>
+__host__ __device__ constexpr bool zshfl_post_ok() {
+  if (!(F::TPL <= 32 && 32 % F::TPL == 0 && (F::LEN / F::RL) % F::TPL == 0)) return false;
+  bool seen[64] = {};
+  if (F::E > 64) return false;
+  for (int s = 0; s < F::E; ++s) {
+    const int a = zslot_a<F>(s);
+    if (a < 0 || a >= F::E || seen[a]) return false;
+    seen[a] = true;
+  }
+  return true;
+}
+template <class F>
+__host__ __device__ constexpr int zslot_of(int a) {
+  for (int s = 0; s < F::E; ++s)
+    if (zslot_a<F>(s) == a) return s;
+  return 0;
+}
+
 // MODE 0: the fused convolution z pass above.
 // MODE 1: the inverse transform of one operand only, its real line (M reals
 //         as H packed pairs) stored to out[line * out_stride + m].
@@ -717,11 +744,38 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
         for (int s = 0; s < E; ++s) v[s] = sm[pidx<LAY>(FF::in_index(t, s))];
       }
       FF::run(v, t, sm, 1, twH, sync);
+      C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
+      if constexpr (zshfl_post_ok<FF>()) {
+        // Z[H - k] from the partner lane by shuffles (no exchange through shared memory)
+        const int lane = threadIdx.x & 31;
+        const int src = (lane & ~(TPL - 1)) + ((TPL - t) & (TPL - 1));
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+          const C give = (t == 0) ? v[zslot_of<FF>((E - q) % E)] : v[zslot_of<FF>(E - 1 - q)];
+          C zc;
+          zc.x = __shfl_sync(0xffffffffu, give.x, src);
+          zc.y = -__shfl_sync(0xffffffffu, give.y, src);
+          const int k = t + TPL * q;
+          const C zk = v[zslot_of<FF>(q)];
+          if (k < a.kout) {
+            const C Ev = mkc<T>(T(0.5) * (zk.x + zc.x), T(0.5) * (zk.y + zc.y));
+            const C Ov = mkc<T>(T(0.5) * (zk.y - zc.y), -T(0.5) * (zk.x - zc.x));
+            dst[k] = cscale(cadd(Ev, cmul(twM[k], Ov)), a.out_scale);
+          }
+        }
+        if (t == 0 && a.kout > H) {  // k = H (kept when kout = H + 1): Z[H] = Z[0]
+          const C zk = v[zslot_of<FF>(0)];
+          const C Ev = mkc<T>(zk.x, T(0));
+          const C Ov = mkc<T>(zk.y, T(0));
+          dst[H] = cscale(cadd(Ev, cmul(twM[H], Ov)), a.out_scale);
+        }
+        __syncthreads();  // stage[st] fully consumed before it is refilled
+        continue;
+      }
       sync();
 #pragma unroll
       for (int s = 0; s < E; ++s) sm[pidx<LAY>(FF::out_index(t, s))] = v[s];
       sync();
-      C* dst = a.out + (long long)(b * LPB + ly) * a.out_stride;
       for (int k = t; k < a.kout; k += TPL) {
         const C zk = sm[pidx<LAY>(k % H)];
         const C zc = cconj(sm[pidx<LAY>((H - k) % H)]);
