@@ -148,6 +148,53 @@ k_colfft3(OP op, const cplx<T>* __restrict__ tw, int ncols) {
   }
 }
 
+// The same staged through shared memory: the first component stays in
+// registers, the other two go to their own tiles as they are loaded, and each
+// later component's transform runs from (and exchanges through) its tile, so
+// registers hold one component and two CTAs share an SM (one's loads overlap
+// the other's transforms).  Every thread reads back only the tile slots it
+// wrote (the first stage's inputs), so no barrier precedes the reads.
+template <typename T, int L, bool INV, int NCOL, class OP, int MINB>
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV>::TPL, MINB)
+k_colfft3s(OP op, const cplx<T>* __restrict__ tw, int ncols) {
+  using F = LineFFT<T, L, INV>;
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* xchg = reinterpret_cast<C*>(smem_raw);  // exchanges of the first component
+  C* tile1 = xchg + L * NCOL;
+  C* tile2 = tile1 + L * NCOL;
+  const int c = threadIdx.x, t = threadIdx.y;
+  const int col = blockIdx.x * NCOL + c;
+  const int slab = blockIdx.y;
+  const bool valid = col < ncols;
+  C v[F::E];
+#pragma unroll
+  for (int s = 0; s < F::E; ++s) {
+    const int e = F::in_index(t, s);
+    C w[3] = {mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0)), mkc<T>(T(0), T(0))};
+    if (valid) op.load3(slab, e, col, w);
+    v[s] = w[0];
+    tile1[e * NCOL + c] = w[1];
+    tile2[e * NCOL + c] = w[2];
+  }
+  F::run(v, t, xchg + c, NCOL, tw, SyncBlock{});
+  if (valid) {
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) op.store(0, slab, F::out_index(t, s), col, v[s]);
+  }
+#pragma unroll
+  for (int d = 1; d < 3; ++d) {
+    C* tl = (d == 1) ? tile1 : tile2;
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) v[s] = tl[F::in_index(t, s) * NCOL + c];
+    F::run(v, t, tl + c, NCOL, tw, SyncBlock{});
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) op.store(d, slab, F::out_index(t, s), col, v[s]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // persistent, double-buffered strided pass.  Each CTA walks tiles
 // (column tile, slab, operand) with stride gridDim.x; while a tile is being

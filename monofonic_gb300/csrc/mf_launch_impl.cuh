@@ -140,6 +140,16 @@ cudaError_t with_conv_geom(const OP& op, LAUNCH&& go) {
   return cudaErrorInvalidValue;
 }
 
+// a plain strided pass of length L launched with compile-time strides when
+// they are those of an x or y pass over an L-grid, else with its own
+template <typename T, int L, class LAUNCH>
+cudaError_t with_plain_axis(const PlainStridedOp<T>& op, LAUNCH&& go) {
+  const long long kz = L / 2 + 1;
+  if (op.e_str == (long long)L * kz && op.slab_str == kz) return go(op.template with_axis<L, 0>());
+  if (op.e_str == kz && op.slab_str == (long long)L * kz) return go(op.template with_axis<L, 1>());
+  return go(op);
+}
+
 template <typename T, int H, class OP>
 cudaError_t launch_zr2c(OP op, int nlines, int kout, const cplx<T>* twH, const cplx<T>* twM, cudaStream_t s) {
   constexpr int LPB = z_lpb<T, H, H + 1>();
@@ -259,10 +269,12 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
 template <typename T>
 cudaError_t Launch<T>::colfft_plain(int L, bool inv, PlainStridedOp<T> op, int nslab, int ncols,
                                     const cplx<T>* tw, cudaStream_t s) {
-#define CASE(LL)                                                              \
-  case LL:                                                                    \
-    return inv ? launch_col<T, LL, true>(op, nslab, ncols, 1, tw, s, KK_FFT_COL)   \
-               : launch_col<T, LL, false>(op, nslab, ncols, 1, tw, s, KK_FFT_COL);
+#define CASE(LL)                                                                     \
+  case LL:                                                                           \
+    return with_plain_axis<T, LL>(op, [&](auto o) {                                  \
+      return inv ? launch_col<T, LL, true>(o, nslab, ncols, 1, tw, s, KK_FFT_COL)      \
+                 : launch_col<T, LL, false>(o, nslab, ncols, 1, tw, s, KK_FFT_COL);    \
+    });
   switch (L) { MF_LEN_N(CASE) default: return cudaErrorInvalidValue; }
 #undef CASE
 }
@@ -296,11 +308,22 @@ cudaError_t launch_col3(Assemble3XInvOp<T> op, int nslab, int ncols, const cplx<
     constexpr int TPL = LineFFT<T, L, true>::TPL;
     constexpr int NC0 = col_ncol<T, L>();
     constexpr int NC = (NC0 * TPL > 512) ? ((512 / TPL) > 0 ? 512 / TPL : 1) : NC0;
+    dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, 1);
+    if (op.n == L && op.Kz == L / 2 + 1) {
+      // the grid as compile-time constants, components staged through shared
+      // memory (two CTAs per SM where three tiles fit twice)
+      const size_t smem = (size_t)3 * L * NC * sizeof(cplx<T>);
+      constexpr int MINB = (2 * 3 * L * NC * (int)sizeof(cplx<T>) <= 200 * 1024 && NC * TPL <= 512) ? 2 : 1;
+      auto kern = k_colfft3s<T, L, true, NC, Assemble3XInvOp<T, L>, MINB>;
+      cudaError_t e = set_smem(kern, smem);
+      if (e != cudaSuccess) return e;
+      kern<<<grid, block, smem, s>>>(op.template with_n<L>(), tw, ncols);
+      return cudaGetLastError();
+    }
     const size_t smem = (size_t)L * NC * sizeof(cplx<T>);
     auto kern = k_colfft3<T, L, true, NC, Assemble3XInvOp<T>>;
     cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
-    dim3 block(NC, TPL), grid((ncols + NC - 1) / NC, nslab, 1);
     kern<<<grid, block, smem, s>>>(op, tw, ncols);
     return cudaGetLastError();
   }

@@ -497,23 +497,43 @@ struct ConvXTruncOp {
 };
 
 // plain strided pass over an n-grid: element (slab, e, col) at
-// base[slab*slab_str + e*e_str + col]; in place, scale on store
-template <typename T>
+// base[slab*slab_str + e*e_str + col]; in place, scale on store.  AXIS 0 / 1
+// with the pass length L: the strides of an x / y pass over an L-grid as
+// compile-time constants (e_str, slab_str = L Kz, Kz or Kz, L Kz with
+// Kz = L/2 + 1); AXIS -1: the run-time strides
+template <typename T, int L = 0, int AXIS = -1>
 struct PlainStridedOp {
   using C = cplx<T>;
   C* p;
   long long e_str, slab_str;
   T scale;
   static constexpr bool kPrefetch = false;
+  static constexpr long long KZ = L / 2 + 1;
+  __device__ __forceinline__ long long es() const {
+    if constexpr (AXIS == 0) return (long long)L * KZ;
+    else if constexpr (AXIS == 1) return KZ;
+    else return e_str;
+  }
+  __device__ __forceinline__ long long ss() const {
+    if constexpr (AXIS == 0) return KZ;
+    else if constexpr (AXIS == 1) return (long long)L * KZ;
+    else return slab_str;
+  }
+  // the op with compile-time strides when they are those of an x (0) or y (1)
+  // pass over an L2-grid
+  template <int L2, int AX2>
+  PlainStridedOp<T, L2, AX2> with_axis() const {
+    return PlainStridedOp<T, L2, AX2>{p, e_str, slab_str, scale};
+  }
   __device__ __forceinline__ C load(int slab, int e, int col) const {
-    return p[(long long)slab * slab_str + (long long)e * e_str + col];
+    return p[(long long)slab * ss() + (long long)e * es() + col];
   }
   __device__ __forceinline__ void store(int slab, int e, int col, C v) const {
-    p[(long long)slab * slab_str + (long long)e * e_str + col] = mkc<T>(v.x * scale, v.y * scale);
+    p[(long long)slab * ss() + (long long)e * es() + col] = mkc<T>(v.x * scale, v.y * scale);
   }
   static constexpr bool kPipe = true;
   __device__ __forceinline__ const C* srcp(int, int slab, int e, int col) const {
-    return p + (long long)slab * slab_str + (long long)e * e_str + col;
+    return p + (long long)slab * ss() + (long long)e * es() + col;
   }
   __device__ __forceinline__ C xform(int, int, int, int, C v) const { return v; }
   __device__ __forceinline__ void store_z(int, int slab, int e, int col, C v) const { store(slab, e, col, v); }
@@ -548,7 +568,7 @@ struct PlainZOp {
 // sub-lattice in one launch: the same k-space combination and sub-lattice
 // phase chain as AssembleXInvOp, with the order sum, the three A3 fields and
 // the gradient read once per mode for the three components
-template <typename T>
+template <typename T, int NN = 0>
 struct Assemble3XInvOp {
   using C = cplx<T>;
   const C* phitot;
@@ -560,7 +580,30 @@ struct Assemble3XInvOp {
   const double* wA;
   int plt, vel;
   const T* pg;  // tabulated PLT gradient and vfac_corr [idx][4]
+  // grid size: NN when the op is specialised to a compile-time n (with_n)
+  __device__ __forceinline__ int nn() const { return NN ? NN : n; }
+  __device__ __forceinline__ int kzn() const { return NN ? NN / 2 + 1 : Kz; }
+  template <int N2>
+  Assemble3XInvOp<T, N2> with_n() const {
+    Assemble3XInvOp<T, N2> o{};
+    o.phitot = phitot;
+    for (int d = 0; d < 3; ++d) {
+      o.A3[d] = A3[d];
+      o.dst[d] = dst[d];
+    }
+    o.n = n;
+    o.Kz = Kz;
+    o.ch = ch;
+    o.kfac = kfac;
+    o.unit = unit;
+    o.wA = wA;
+    o.plt = plt;
+    o.vel = vel;
+    o.pg = pg;
+    return o;
+  }
   __device__ __forceinline__ void assemble(int i, int j, int kz, C (&o)[3]) const {
+    const int n = nn(), Kz = kzn();
     const long long idx = ((long long)i * n + j) * Kz + kz;
     if (idx == 0) {
       o[0] = o[1] = o[2] = mkc<T>(T(0), T(0));
@@ -604,6 +647,7 @@ struct Assemble3XInvOp {
   }
   // slab = j, e = i, col = kz
   __device__ __forceinline__ void load3(int j, int i, int kz, C (&v)[3]) const {
+    const int n = nn();
     assemble(i, j, kz, v);
     if (ch.nstep == 0) return;
     C vm[3];
@@ -611,7 +655,7 @@ struct Assemble3XInvOp {
     ch.template apply<3>(n, i, j, kz, v, vm);
   }
   __device__ __forceinline__ void store(int d, int j, int i, int kz, C v) const {
-    dst[d][((long long)i * n + j) * Kz + kz] = v;
+    dst[d][((long long)i * nn() + j) * kzn() + kz] = v;
   }
 };
 
