@@ -166,11 +166,13 @@ def algorithmic_bytes_ic(n: int, prec_bytes: int, overload: int = 2, plt: bool =
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch from
-# ncu captures of smaller cases, per unit of work (M^2 (N/2+1) line-modes of
-# the padded work buffer), so that it scales to the bench's grid size
+# an ncu capture, per unit of work (M^3 of the padded transform), so that it
+# scales to other grid sizes; measured at the bench's N=512
 TRAFFIC_PER_UNIT = {
-    ("conv_z", 4): (325.9e6 / (384 * 384 * 384), "ncu --set full, k_zconv_tma (c2r of one operand into a real "
-                                                 "padded field) N=256 (M=384) FP32, one launch"),
+    ("conv_z", 4): (2.971e9 / (768 * 768 * 768), "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,"
+                                                 "gpu__time_duration.sum (one pass per launch): the 27 k_zconv_tma "
+                                                 "launches of one 3LPT BCC IC at N=512 (M=768), FP32 (17 operand "
+                                                 "c2r 2.967 GB, 10 product-sum r2c 2.979 GB per launch), mean"),
 }
 
 
@@ -179,7 +181,7 @@ def traffic_per_launch(kind: str, n: int, prec_bytes: int):
     if t is None:
         return None, None
     M = 3 * n // 2
-    return t[0] * M * M * M, t[1] + f", scaled to N={n} by M^3"
+    return t[0] * M * M * M, t[1] + ("" if n == 512 else f", scaled to N={n} by M^3")
 
 
 def measured_peaks():
