@@ -517,7 +517,12 @@ __device__ __forceinline__ void lattice_line_out(Lattice3Args a, int line, int t
 template <typename T, int H, int LPB, typename P>
 __global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H, true>::E <= 8) ? 2 : 1)
     k_zc2r3_lattice(Lattice3Args a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
-  using F = LineFFT<T, H, true>;
+  // each line's exchanges run in its own staged region (XOR layout of the
+  // contiguous-line passes), under warp barriers when a line's threads sit
+  // inside one warp
+  // (the identity layout where three components of E > 8 values already fill the registers)
+  using F = LineFFT<T, H, true, 8, (LineFFT<T, H, true>::E <= 8) ? zlayout(H) : 0>;
+  using SYNC = typename std::conditional<(F::TPL <= 32 && 32 % F::TPL == 0), SyncWarp, SyncBlock>::type;
   using C = cplx<T>;
   constexpr int SL = 3 * (H + 1);  // complex values of one line's three components
   // persistent CTAs over batches of LPB lines; the next batch is copied into
@@ -564,7 +569,7 @@ __global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H,
 #pragma unroll
       for (int s = 0; s < F::E; ++s) v[d][s] = c2r_pre<T, H>(sm[d], F::in_index(t, s), twM);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) F::run(v[d], t, sm[d], 1, twH, SyncBlock{});
+    for (int d = 0; d < 3; ++d) F::run(v[d], t, sm[d], 1, twH, SYNC{});
     if (valid) lattice_line_out<T, H, P>(a, line, t, v);
     __syncthreads();  // cur is refilled by the next iteration's copies
   }
