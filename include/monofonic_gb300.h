@@ -197,10 +197,10 @@ int mf_conv_convolve2_invlap(mf_conv* cv, const mf_operand* a, const mf_operand*
  * precision); the padded work buffers live in one static 48 MiB device array
  * that the library holds on every device it is loaded on, which limits this
  * call to n <= 128 (FP32) and n <= 96 (FP64); larger sizes return
- * MF_ERR_SHAPE.  The first call on a device looks up that array's device
- * address and should come before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race; the call returns when the
- * result is complete (MF_ERR_TIMEOUT if a bounded wait ran out).  kind_a /
+ * MF_ERR_SHAPE.  All calls share the array, so calls that overlap on the
+ * GPU race.  The call synchronises the stream and reads the device error flag
+ * before it returns (the result is then complete; MF_ERR_TIMEOUT if a bounded
+ * wait ran out), so it cannot be recorded into a CUDA graph.  kind_a /
  * kind_b are MF_OPND_* with directions dirs_a / dirs_b (4 ints each), op is
  * MF_OP_* applied to out with factor x. */
 int mf_conv_convolve2_noalloc(void* stream, int n, double boxlen, int prec, const void* field_a, int kind_a,
