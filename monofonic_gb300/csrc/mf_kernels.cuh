@@ -283,6 +283,101 @@ k_colfft_pipe(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nsl
 }
 
 // ---------------------------------------------------------------------------
+// The same pass with one column per line group inside a warp (a build-time
+// variant, MF_COL_WPC): the tile is staged column-major ([column][row], column
+// stride LSC = 4 mod 16 elements, so the row-major staging copies and the
+// copy-out reads take the minimum number of wavefronts), each column's
+// transform exchanges through its own column under warp barriers (the XOR
+// layout of the contiguous-line passes), and the results go back to global
+// memory in 64-byte row runs from a column-major copy-out.  Ops with a
+// prefetched read-modify-write target are not eligible.
+// ---------------------------------------------------------------------------
+template <typename T, int L, bool INV>
+__host__ __device__ constexpr int wpc_lsc() {
+  constexpr int base = padded_len(L, zlayout(L));
+  return base + ((4 - base % 16) % 16 + 16) % 16;
+}
+template <typename T, int L, bool INV, class OP>
+__host__ __device__ constexpr bool wpc_ok() {
+  using F = LineFFT<T, L, INV, MF_COL_MAXR>;
+  return !OP::kPrefetch && F::TPL <= 32 && 32 % F::TPL == 0;
+}
+template <typename T, int L, bool INV, int NCOL, class OP>
+__global__ void __launch_bounds__(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
+                                  col_minb(NCOL * LineFFT<T, L, INV, MF_COL_MAXR>::TPL,
+                                           LineFFT<T, L, INV, MF_COL_MAXR>::E, (int)sizeof(T)))
+k_colfft_wpc(OP op, const cplx<T>* __restrict__ tw, int ncols, int ntc, int nslab, int nz) {
+  using F = LineFFT<T, L, INV, MF_COL_MAXR, zlayout(L)>;
+  using C = cplx<T>;
+  constexpr int LSC = wpc_lsc<T, L, INV>();
+  constexpr int NT = NCOL * F::TPL;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf0 = reinterpret_cast<C*>(smem_raw);
+  C* buf1 = buf0 + NCOL * LSC;
+  const int tid = threadIdx.x;
+  const int cl = tid / F::TPL, t = tid % F::TPL;  // this thread's column in the tile and its line slot
+  const int total = ntc * nslab * nz;
+  auto issue = [&](int tl, C* buf) {
+    const int ct = tl % ntc, r = tl / ntc, slab = r % nslab, z = r / nslab;
+#pragma unroll 4
+    for (int u = tid; u < L * NCOL; u += NT) {
+      const int e = u / NCOL, c = u % NCOL;
+      const int col = ct * NCOL + c;
+      C* d = buf + c * LSC + e;
+      const C* g = (col < ncols) ? op.srcp(z, slab, e, col) : nullptr;
+      if (g) {
+        if constexpr (sizeof(C) == 16) cp_async16(d, g); else cp_async8(d, g);
+      } else {
+        *d = mkc<T>(T(0), T(0));
+      }
+    }
+    cp_async_commit();
+  };
+  int tl = blockIdx.x;
+  if (tl < total) issue(tl, buf0); else cp_async_commit();
+  for (int it = 0; tl < total; tl += gridDim.x, ++it) {
+    C* cur = (it & 1) ? buf1 : buf0;
+    C* nxt = (it & 1) ? buf0 : buf1;
+    const int tn = tl + gridDim.x;
+    if (tn < total) issue(tn, nxt); else cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();  // every thread's copies of this tile have landed
+    const int ct = tl % ntc, r = tl / ntc, slab = r % nslab, z = r / nslab;
+    const int col = ct * NCOL + cl;
+    const bool valid = col < ncols;
+    C* cb = cur + cl * LSC;
+    C v[F::E];
+    if constexpr (has_tile_prep<OP>::value) {
+      const auto tp = op.tile_prep(z, slab, col);
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) {
+        const int e = F::in_index(t, s);
+        v[s] = valid ? op.xform_tile(tp, e, cb[e]) : mkc<T>(T(0), T(0));
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < F::E; ++s) {
+        const int e = F::in_index(t, s);
+        v[s] = valid ? op.xform(z, slab, e, col, cb[e]) : mkc<T>(T(0), T(0));
+      }
+    }
+    F::run(v, t, cb, 1, tw, SyncWarp{});
+    __syncwarp();  // the column's last exchange has been read
+#pragma unroll
+    for (int s = 0; s < F::E; ++s) cb[F::out_index(t, s)] = v[s];
+    __syncthreads();  // every column of the tile is transformed
+#pragma unroll 4
+    for (int u = tid; u < L * NCOL; u += NT) {
+      const int e = u / NCOL, c = u % NCOL;
+      const int cc = ct * NCOL + c;
+      if (cc < ncols) op.store_z(z, slab, e, cc, cur[c * LSC + e]);
+    }
+    __syncthreads();  // cur is refilled by the next iteration's copies
+  }
+  cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 // strided forward transform, truncation and inverse transform of one column in
 // one pass (ConvXTruncOp), persistent and double-buffered as k_colfft_pipe
 // ---------------------------------------------------------------------------

@@ -75,9 +75,34 @@ constexpr int pipe_ncol() {
   return nc;
 }
 
+// 1: the pipelined strided passes with one column per warp where eligible
+// (k_colfft_wpc; a build-time knob)
+#ifndef MF_COL_WPC
+#define MF_COL_WPC 0
+#endif
+
 template <typename T, int L, bool INV, class OP>
 cudaError_t launch_col(OP op, int nslab, int ncols, int nz, const cplx<T>* tw, cudaStream_t s, int kind) {
-  if constexpr (OP::kPipe && MF_COL_PIPE) {
+  if constexpr (OP::kPipe && MF_COL_PIPE && MF_COL_WPC && wpc_ok<T, L, INV, OP>()) {
+    constexpr int NC = pipe_ncol<T, L>();
+    constexpr int TPL = LineFFT<T, L, INV, MF_COL_MAXR>::TPL;
+    const size_t smem = (size_t)2 * NC * wpc_lsc<T, L, INV>() * sizeof(cplx<T>);
+    auto kern = k_colfft_wpc<T, L, INV, NC, OP>;
+    cudaError_t e = set_smem(kern, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NC * TPL, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int ntc = (ncols + NC - 1) / NC;
+    const int total = ntc * nslab * nz;
+    int grid = nsm * per_sm;
+    if (grid > total) grid = total;
+    kern<<<grid, NC * TPL, smem, s>>>(op, tw, ncols, ntc, nslab, nz);
+    return cudaGetLastError();
+  } else if constexpr (OP::kPipe && MF_COL_PIPE) {
     constexpr int NC = pipe_ncol<T, L>();
     constexpr int TPL = LineFFT<T, L, INV, MF_COL_MAXR>::TPL;
     const size_t smem = (size_t)2 * L * NC * sizeof(cplx<T>);
