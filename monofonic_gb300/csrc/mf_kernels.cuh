@@ -804,8 +804,21 @@ __host__ __device__ constexpr int zslot_of(int a) {
 //         as H packed pairs) stored to out[line * out_stride + m].
 // MODE 2: the forward transform of one real line (H packed pairs, kin = H),
 //         stored as kz < kout like MODE 0.
+// CTAs per SM the FP32 r2c z pass (MODE 2) is compiled for: it exchanges in
+// its staged input lines, so four fit by shared memory at 128 registers
+// (0 elsewhere: no minimum, the compiler's register choice)
+template <typename T, int MODE>
+__host__ __device__ constexpr int zconv_tma_minb() {
+  return sizeof(T) != 4 ? 0 : (MODE == 2 ? 4 : 0);
+}
+// the r2c mode exchanges in its staged input lines (kin = H) when the
+// exchange stride of a line fits in one
+template <int H, int MODE>
+__host__ __device__ constexpr bool zconv_xchg_in_stage() {
+  return MODE == 2 && zline_stride(H) <= H;
+}
 template <typename T, int H, int MAXR, int LPB, class SYNC, int MODE = 0>
-__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL)
+__global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL, zconv_tma_minb<T, MODE>())
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
   constexpr int LAY = zlayout(H);
   using FI = LineFFT<T, H, true, MAXR, LAY, true>;
@@ -820,7 +833,7 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
   const int per_op = LPB * kin;
   C* xchg = stage + 2 * nop * per_op;
   const int t = threadIdx.x % TPL, ly = threadIdx.x / TPL;
-  C* sm = xchg + ly * LS;
+  C* const sm_x = xchg + ly * LS;
   const int nbatch = a.nlines / LPB;
   const unsigned bytes_op = (unsigned)(per_op * sizeof(C));
   const C* in0 = a.in[0];
@@ -858,6 +871,9 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
       return;
     }
     C v[E], prod[E];
+    // this line's exchange area: its staged input line in the r2c mode (read
+    // into registers before the transform's first exchange), else its own
+    C* const sm = zconv_xchg_in_stage<H, MODE>() ? stage + (st * nop) * per_op + ly * kin : sm_x;
     if constexpr (MODE == 2) {
       const C* src = stage + (st * nop) * per_op + ly * kin;
 #pragma unroll

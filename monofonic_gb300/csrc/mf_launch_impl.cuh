@@ -239,7 +239,8 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     if (tma_ok) {
       auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE>;
       const size_t smem =
-          128 + ((size_t)2 * a.nop * LPBT * a.kin + (size_t)LPBT * zline_stride(H)) * sizeof(cplx<T>);
+          128 + ((size_t)2 * a.nop * LPBT * a.kin + (zconv_xchg_in_stage<H, MODE>() ? 0 : (size_t)LPBT * zline_stride(H))) *
+                    sizeof(cplx<T>);
       cudaError_t e = set_smem(kern, smem);
       if (e != cudaSuccess) return e;
       int per_sm = 0, nsm = 0, dev = 0;
