@@ -455,6 +455,8 @@ __global__ void __launch_bounds__(NT) k_zr2c(OP op, const cplx<T>* __restrict__ 
                                                const cplx<T>* __restrict__ twM, int nlines, int kout) {
   using F = LineFFT<T, H, false>;
   using C = cplx<T>;
+  // a line's shared-memory area is its own: warp barriers when its threads sit inside one warp
+  using SYNC = typename std::conditional<(F::TPL <= 32 && 32 % F::TPL == 0 && NT % 32 == 0), SyncWarp, SyncBlock>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = threadIdx.x, ly = threadIdx.y;
   const int line = blockIdx.x * blockDim.y + ly;
@@ -463,11 +465,11 @@ __global__ void __launch_bounds__(NT) k_zr2c(OP op, const cplx<T>* __restrict__ 
   C v[F::E];
 #pragma unroll
   for (int s = 0; s < F::E; ++s) v[s] = valid ? op.load_pair(line, F::in_index(t, s)) : mkc<T>(T(0), T(0));
-  F::run(v, t, sm, 1, twH, SyncBlock{});
-  __syncthreads();
+  F::run(v, t, sm, 1, twH, SYNC{});
+  SYNC{}();
 #pragma unroll
   for (int s = 0; s < F::E; ++s) sm[F::out_index(t, s)] = v[s];
-  __syncthreads();
+  SYNC{}();
   if (valid) {
     for (int k = t; k < kout; k += F::TPL) {
       const C zk = sm[k % H];
@@ -501,17 +503,19 @@ __global__ void __launch_bounds__(NT) k_zc2r(OP op, const cplx<T>* __restrict__ 
                                                const cplx<T>* __restrict__ twM, int nlines, int kin) {
   using F = LineFFT<T, H, true>;
   using C = cplx<T>;
+  // a line's shared-memory area is its own: warp barriers when its threads sit inside one warp
+  using SYNC = typename std::conditional<(F::TPL <= 32 && 32 % F::TPL == 0 && NT % 32 == 0), SyncWarp, SyncBlock>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = threadIdx.x, ly = threadIdx.y;
   const int line = blockIdx.x * blockDim.y + ly;
   const bool valid = line < nlines;
   C* sm = reinterpret_cast<C*>(smem_raw) + ly * (H + 1);
   for (int k = t; k <= H; k += F::TPL) sm[k] = (valid && k < kin) ? op.load(line, k) : mkc<T>(T(0), T(0));
-  __syncthreads();
+  SYNC{}();
   C v[F::E];
 #pragma unroll
   for (int s = 0; s < F::E; ++s) v[s] = c2r_pre<T, H>(sm, F::in_index(t, s), twM);
-  F::run(v, t, sm, 1, twH, SyncBlock{});
+  F::run(v, t, sm, 1, twH, SYNC{});
   if (valid) {
 #pragma unroll
     for (int s = 0; s < F::E; ++s) op.store_pair(line, F::out_index(t, s), v[s]);
@@ -617,7 +621,8 @@ __global__ void __launch_bounds__(LPB * LineFFT<T, H, true>::TPL, (LineFFT<T, H,
   // inside one warp
   // (the identity layout where three components of E > 8 values already fill the registers)
   using F = LineFFT<T, H, true, 8, (LineFFT<T, H, true>::E <= 8) ? zlayout(H) : 0>;
-  using SYNC = typename std::conditional<(F::TPL <= 32 && 32 % F::TPL == 0), SyncWarp, SyncBlock>::type;
+  using SYNC = typename std::conditional<(F::TPL <= 32 && 32 % F::TPL == 0 && (LPB * F::TPL) % 32 == 0), SyncWarp,
+                                         SyncBlock>::type;
   using C = cplx<T>;
   constexpr int SL = 3 * (H + 1);  // complex values of one line's three components
   // persistent CTAs over batches of LPB lines; the next batch is copied into
