@@ -818,8 +818,7 @@ def write_detail(args, detail) -> str | None:
     the one printed line, goes to a side file"""
     path = args.detail
     if path is None:
-        out = os.path.join(ROOT, "gpurun_out")
-        path = os.path.join(out if os.path.isdir(out) else tempfile.gettempdir(), "bench_detail.json")
+        path = os.path.join(tempfile.gettempdir(), "bench_detail.json")
     try:
         with open(path, "w") as f:
             json.dump(detail, f, indent=1)
