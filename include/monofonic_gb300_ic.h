@@ -157,7 +157,10 @@ int mf_ic_run(mf_ic* ic, mf_particles* out);
  * after this call likewise overlaps this run.  The host buffers are complete,
  * and the host noise buffers of the queued runs may be reused, once
  * mf_ic_wait (or a synchronous run) returns.  Device errors of the queued
- * runs are reported there. */
+ * runs are reported there.  Runs into host buffers (this call, and
+ * mf_ic_run with MF_LOC_HOST) are refused with MF_ERR_STATE while the
+ * context's stream is being captured into a CUDA graph: record
+ * mf_ic_enqueue instead. */
 int mf_ic_run_async(mf_ic* ic, const mf_particles* out);
 /* wait for every queued run of the pipeline, its host copies included */
 int mf_ic_wait(mf_ic* ic);

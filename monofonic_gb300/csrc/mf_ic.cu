@@ -1515,6 +1515,16 @@ bool host_buffers(const mf_ic* ic, const mf_particles* out) {
   return out && out->location == MF_LOC_HOST && out->pos && out->vel &&
          (ic->p.out_kind == MF_OUT_FIELDS || out->ids);
 }
+
+// a host hand-off runs on a second stream and cannot be recorded into a graph
+int refuse_capture(mf_ic* ic, const char* where) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(ic->ctx->stream, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ic->ctx, MF_ERR_STATE, where);
+  }
+  return st == cudaStreamCaptureStatusNone ? MF_OK : set_err(ic->ctx, MF_ERR_STATE, where);
+}
 }  // namespace
 
 extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
@@ -1523,7 +1533,8 @@ extern "C" int mf_ic_run(mf_ic* ic, mf_particles* out) {
   if (!ic->noise_set && !ic->noise_seeded) return set_err(ic->ctx, MF_ERR_STATE, "mf_ic_run: white noise not set");
   reset_early(ic);
   if (host_buffers(ic, out)) {
-    const int rc = make_copy_stream(ic, "mf_ic_run: copy stream");
+    int rc = refuse_capture(ic, "mf_ic_run: a run into host buffers cannot be captured (use mf_ic_enqueue)");
+    if (rc == MF_OK) rc = make_copy_stream(ic, "mf_ic_run: copy stream");
     if (rc != MF_OK) return rc;
     ic->early = out;
   }
@@ -1542,7 +1553,8 @@ extern "C" int mf_ic_run_async(mf_ic* ic, const mf_particles* out) {
   if (ic->p.baryons) return set_err(c, MF_ERR_ARG, "mf_ic_run_async: a two-species pipeline runs with mf_ic_run_species");
   if (!host_buffers(ic, out)) return set_err(c, MF_ERR_ARG, "mf_ic_run_async: host buffers expected");
   if (!ic->noise_set && !ic->noise_seeded) return set_err(c, MF_ERR_STATE, "mf_ic_run_async: white noise not set");
-  int rc = make_copy_stream(ic, "mf_ic_run_async: copy stream");
+  int rc = refuse_capture(ic, "mf_ic_run_async: a run into host buffers cannot be captured (use mf_ic_enqueue)");
+  if (rc == MF_OK) rc = make_copy_stream(ic, "mf_ic_run_async: copy stream");
   if (rc != MF_OK) return rc;
   reset_early(ic);
   ic->early_out = *out;

@@ -160,3 +160,33 @@ def test_host_noise_after_stage_times_of_a_device_run(ctx):
     pin.close()
     host.close()
     g.close()
+
+
+def test_host_runs_refused_while_capturing(ctx):
+    """a run into host buffers streams its copies on a second stream, so it
+    is refused (MF_ERR_STATE, nothing enqueued) while the context's stream is
+    being captured into a CUDA graph; the capture and the pipeline stay usable"""
+    import ctypes as C
+    import warnings
+    import torch
+    import monofonic_gb300 as mf
+    from monofonic_gb300 import _lib as Lb
+    g = _pipeline(ctx)
+    g.set_noise_seed(3)
+    host = _HostSet(g)
+    out = Lb.mf_particles()
+    out.pos, out.vel, out.ids = host.ptrs
+    out.location = Lb.MF_LOC_HOST
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", 0))
+    graph = torch.cuda.CUDAGraph()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")  # the captured graph is empty
+        with torch.cuda.graph(graph, stream=stream):
+            rc_async = mf.lib().mf_ic_run_async(g.ptr, C.byref(out))
+            rc_sync = mf.lib().mf_ic_run(g.ptr, C.byref(out))
+    assert rc_async == Lb.MF_ERR_STATE and rc_sync == Lb.MF_ERR_STATE
+    g.run_into(*host.ptrs)
+    pos, vel, ids = host.arrays()
+    assert np.all(np.isfinite(pos)) and ids[0] == 0
+    host.close()
+    g.close()
