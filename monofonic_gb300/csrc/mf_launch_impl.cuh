@@ -232,7 +232,8 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     // build-time knob: more, smaller CTAs per SM)
     constexpr int LPB0 = tma_lines_per_batch<T, TPL>();
     constexpr int LPBT = (MODE != 0 && LPB0 >= 2 * MF_ZONE_LPB_DIV) ? LPB0 / MF_ZONE_LPB_DIV : LPB0;
-    const bool tma_ok = MF_ZCONV_TMA && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
+    // (the r2c mode's lines hold H pairs; its exchanges run in them when they fit)
+    const bool tma_ok = MF_ZCONV_TMA && (MODE != 2 || a.kin == H) && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
                         (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
                         (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
