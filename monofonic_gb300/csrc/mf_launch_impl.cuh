@@ -18,9 +18,14 @@
 #ifndef MF_ZCONV_TMA
 #define MF_ZCONV_TMA 1
 #endif
-// divisor of the lines per batch of the one-transform TMA z passes (a build-time knob)
+// divisors of the lines per batch of the one-transform TMA z passes (build-time
+// knobs): at N=512 quarter batches were 2 % faster for the c2r (MODE 1) and
+// 8 % slower for the r2c (MODE 2) than half batches
 #ifndef MF_ZONE_LPB_DIV
 #define MF_ZONE_LPB_DIV 2
+#endif
+#ifndef MF_ZC2R_LPB_DIV
+#define MF_ZC2R_LPB_DIV 4
 #endif
 // largest radix of the TMA z pass plan (8: fewer exchanges, more registers)
 #ifndef MF_ZCONV_TMA_MAXR
@@ -231,7 +236,8 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     // lines per batch; the one-transform modes may use a fraction of it (a
     // build-time knob: more, smaller CTAs per SM)
     constexpr int LPB0 = tma_lines_per_batch<T, TPL>();
-    constexpr int LPBT = (MODE != 0 && LPB0 >= 2 * MF_ZONE_LPB_DIV) ? LPB0 / MF_ZONE_LPB_DIV : LPB0;
+    constexpr int DIV = (MODE == 1) ? MF_ZC2R_LPB_DIV : MF_ZONE_LPB_DIV;
+    constexpr int LPBT = (MODE != 0 && LPB0 >= 2 * DIV) ? LPB0 / DIV : LPB0;
     // (the r2c mode's lines hold H pairs; its exchanges run in them when they fit)
     const bool tma_ok = MF_ZCONV_TMA && (MODE != 2 || a.kin == H) && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
                         (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
