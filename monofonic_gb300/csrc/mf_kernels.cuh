@@ -917,8 +917,12 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
         // Z[H - k] from the partner lane by shuffles (no exchange through shared memory)
         const int lane = threadIdx.x & 31;
         const int src = (lane & ~(TPL - 1)) + ((TPL - t) & (TPL - 1));
+        // slots that can hold a kept k: the r2c mode keeps kz <= 2H/3 (the
+        // Orszag N/2, checked at launch), the fused pass up to H
+        constexpr int QK = (MODE == 2) ? (2 * H / 3 + 1 + TPL - 1) / TPL : E;
+        constexpr int QMAX = QK < E ? QK : E;
 #pragma unroll
-        for (int q = 0; q < E; ++q) {
+        for (int q = 0; q < QMAX; ++q) {
           const C give = (t == 0) ? v[zslot_of<FF>((E - q) % E)] : v[zslot_of<FF>(E - 1 - q)];
           C zc;
           zc.x = __shfl_sync(0xffffffffu, give.x, src);

@@ -239,7 +239,8 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
     constexpr int DIV = (MODE == 1) ? MF_ZC2R_LPB_DIV : MF_ZONE_LPB_DIV;
     constexpr int LPBT = (MODE != 0 && LPB0 >= 2 * DIV) ? LPB0 / DIV : LPB0;
     // (the r2c mode's lines hold H pairs; its exchanges run in them when they fit)
-    const bool tma_ok = MF_ZCONV_TMA && (MODE != 2 || a.kin == H) && (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
+    const bool tma_ok = MF_ZCONV_TMA && (MODE != 2 || (a.kin == H && a.kout <= 2 * H / 3 + 1)) &&
+                        (a.nlines % LPBT == 0) && (a.in_stride == a.kin) &&
                         (((size_t)LPBT * a.kin * sizeof(cplx<T>)) % 16 == 0) &&
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
                         (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
