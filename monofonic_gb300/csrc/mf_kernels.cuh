@@ -822,7 +822,7 @@ template <int H, int MODE>
 __host__ __device__ constexpr bool zconv_xchg_in_stage() {
   return MODE == 2 && zline_stride(H) <= H;
 }
-template <typename T, int H, int MAXR, int LPB, class SYNC, int MODE = 0>
+template <typename T, int H, int MAXR, int LPB, class SYNC, int MODE = 0, int KIN = 0>
 __global__ void __launch_bounds__(LPB * LineFFT<T, H, true, MAXR>::TPL, zconv_tma_minb<T, MODE>())
 k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __restrict__ twM) {
   constexpr int LAY = zlayout(H);
@@ -833,7 +833,8 @@ k_zconv_tma(ZConvArgs<T> a, const cplx<T>* __restrict__ twH, const cplx<T>* __re
   constexpr int LS = zline_stride(H);  // per-line exchange length
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
-  const int nop = a.nop, kin = a.kin;
+  const int nop = (MODE == 0) ? a.nop : 1;
+  const int kin = KIN ? KIN : a.kin;  // line length (compiled in when KIN > 0)
   C* stage = reinterpret_cast<C*>(smem_raw + 128);
   const int per_op = LPB * kin;
   C* xchg = stage + 2 * nop * per_op;

@@ -245,7 +245,12 @@ cudaError_t launch_zconv(const ZConvArgs<T>& a, const cplx<T>* twH, const cplx<T
                         ((uintptr_t)a.in[0] % 16 == 0) && (a.nop < 2 || (uintptr_t)a.in[1] % 16 == 0) &&
                         (a.nop < 3 || (uintptr_t)a.in[2] % 16 == 0);
     if (tma_ok) {
-      auto kern = k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE>;
+      // the c2r of one Orszag operand with its line length (kz <= N/2, 2H/3 + 1)
+      // compiled in: 0.561 -> 0.520 ms per launch at N=512 (the r2c with its H
+      // pairs compiled in measured no faster)
+      constexpr int KIN_CT = (MODE == 1 && H % 3 == 0) ? 2 * H / 3 + 1 : 0;
+      auto kern = (KIN_CT != 0 && a.kin == KIN_CT) ? k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE, KIN_CT>
+                                                   : k_zconv_tma<T, H, MAXR, LPBT, SYNC, MODE, 0>;
       const size_t smem =
           128 + ((size_t)2 * a.nop * LPBT * a.kin + (zconv_xchg_in_stage<H, MODE>() ? 0 : (size_t)LPBT * zline_stride(H))) *
                     sizeof(cplx<T>);
